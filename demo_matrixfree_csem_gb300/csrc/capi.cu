@@ -1,0 +1,421 @@
+// extern "C" entry points of libcsem_gpu.so (declared in include/csem_gpu.h).
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+#include "../../include/csem_gpu.h"
+#include "engine_model.h"
+#include "solve_fp64.h"
+
+extern "C" int csem_set_error(int code, const char* fmt, ...);
+
+using namespace csem;
+
+struct csem_ctx {
+  Model* model = nullptr;
+  cudaStream_t st = nullptr;
+  Ops<F64>* ops64 = nullptr;
+  Ops<F32>* ops32 = nullptr;
+  Solver64* solver = nullptr;
+  DevBuf io[4], sc64, sc32, dotp;
+  int nmax64 = 0, nmax32 = 0;
+};
+
+#define API_BEGIN try {
+#define API_END                                                                                          \
+  }                                                                                                      \
+  catch (const CudaError& e) {                                                                           \
+    return csem_set_error(CSEM_ECUDA, "CUDA error %d (%s) in %s at %s:%d", (int)e.err,                  \
+                          cudaGetErrorString(e.err), e.expr, e.file, e.line);                            \
+  }                                                                                                      \
+  catch (const std::bad_alloc&) {                                                                        \
+    return csem_set_error(CSEM_ENOMEM, "host allocation failed");                                        \
+  }                                                                                                      \
+  return CSEM_OK;
+
+static Ops<F64>* ops64_for(csem_ctx* c, int nsys)
+{
+  if (!c->ops64 || c->nmax64 < nsys) {
+    delete c->ops64;
+    c->ops64 = new Ops<F64>(c->model, nsys, c->st);
+    c->nmax64 = nsys;
+  }
+  return c->ops64;
+}
+
+static Ops<F32>* ops32_for(csem_ctx* c, int nsys)
+{
+  if (!c->ops32 || c->nmax32 < nsys) {
+    delete c->ops32;
+    c->ops32 = new Ops<F32>(c->model, nsys, c->st);
+    c->nmax32 = nsys;
+  }
+  return c->ops32;
+}
+
+static void ensure(DevBuf& b, size_t bytes)
+{
+  if (b.bytes < bytes) b.alloc(bytes);
+}
+
+// per-system scalars from host (re,im) pairs
+static void upload_scal(csem_ctx* c, int nsys, const double* iom)
+{
+  std::vector<SysScal<F64>> s64(nsys);
+  std::vector<SysScal<F32>> s32(nsys);
+  for (int q = 0; q < nsys; q++) {
+    s64[q] = sys_scal64(iom[2 * q], iom[2 * q + 1]);
+    s32[q] = sys_scal32(s64[q]);
+  }
+  ensure(c->sc64, sizeof(SysScal<F64>) * nsys);
+  ensure(c->sc32, sizeof(SysScal<F32>) * nsys);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->sc64.p, s64.data(), sizeof(SysScal<F64>) * nsys, cudaMemcpyHostToDevice, c->st));
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->sc32.p, s32.data(), sizeof(SysScal<F32>) * nsys, cudaMemcpyHostToDevice, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+}
+
+extern "C" {
+
+const char* csem_version(void) { return "csem-gb300 0.1 (sm_103a)"; }
+
+int csem_device_count(void)
+{
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int csem_ctx_create(const csem_grid_t* g, int airbc, int fvm, csem_ctx** out)
+{
+  *out = nullptr;
+  if (csem_device_count() < 1) return csem_set_error(CSEM_ENODEV, "no CUDA device available");
+  if (!g || !g->sigma11) return csem_set_error(CSEM_EINVAL, "grid is not extended (csem_grid_extend)");
+  if (airbc && (g->nb <= 0 || !g->sH1))
+    return csem_set_error(CSEM_EINVAL, "airbc=1 needs nb>0 and the airwave tables (csem_grid_airbc)");
+  API_BEGIN
+  std::unique_ptr<csem_ctx> c(new csem_ctx());
+  CSEM_CUDA_TRY(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  c->model = new Model((const csem_grid*)g, airbc, fvm);
+  *out = c.release();
+  API_END
+}
+
+void csem_ctx_destroy(csem_ctx* c)
+{
+  if (!c) return;
+  cudaStreamSynchronize(c->st);
+  delete c->solver;
+  delete c->ops64;
+  delete c->ops32;
+  delete c->model;
+  for (auto& b : c->io) b.free_();
+  c->sc64.free_();
+  c->sc32.free_();
+  c->dotp.free_();
+  cudaStreamDestroy(c->st);
+  delete c;
+}
+
+int csem_ctx_sizes(const csem_ctx* c, long* o)
+{
+  const Model* m = c->model;
+  o[0] = m->lE; o[1] = m->lEx; o[2] = m->lEy; o[3] = m->lEz; o[4] = m->lv;
+  o[5] = m->n1; o[6] = m->n2; o[7] = m->n3; o[8] = m->n3f; o[9] = m->nb;
+  return CSEM_OK;
+}
+
+int csem_ctx_sync(csem_ctx* c)
+{
+  API_BEGIN
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  API_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- host-buffer operators
+enum { OP_A = 0, OP_LUSGS = 1, OP_APHI = 2 };
+
+template <class P>
+static int op_host(csem_ctx* c, int op, double re, double im, const void* x, void* y)
+{
+  typedef typename P::C C;
+  const long n = c->model->lE;
+  const size_t bytes = sizeof(C) * (size_t)n;
+  ensure(c->io[0], bytes);
+  ensure(c->io[1], bytes);
+  double iom[2] = {re, im};
+  upload_scal(c, 1, iom);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[0].p, x, bytes, cudaMemcpyHostToDevice, c->st));
+  C* X = c->io[0].as<C>();
+  C* Y = c->io[1].as<C>();
+  if (P::exact) {
+    Ops<F64>* o = ops64_for(c, 1);
+    const SysScal<F64>* s = c->sc64.as<SysScal<F64>>();
+    if (op == OP_A) o->apply_A((double2*)X, (double2*)Y, 1, nullptr, s);
+    else if (op == OP_LUSGS) o->apply_lusgs((double2*)X, (double2*)Y, 1, nullptr, s);
+    else o->apply_aphi((double2*)X, (double2*)Y, 1, nullptr, s);
+  } else {
+    Ops<F32>* o = ops32_for(c, 1);
+    const SysScal<F32>* s = c->sc32.as<SysScal<F32>>();
+    if (op == OP_A) o->apply_A((float2*)X, (float2*)Y, 1, nullptr, s);
+    else if (op == OP_LUSGS) o->apply_lusgs((float2*)X, (float2*)Y, 1, nullptr, s);
+    else o->apply_aphi((float2*)X, (float2*)Y, 1, nullptr, s);
+  }
+  CSEM_CUDA_TRY(cudaGetLastError());
+  CSEM_CUDA_TRY(cudaMemcpyAsync(y, Y, bytes, cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return CSEM_OK;
+}
+
+template <class P>
+static int cdot_host(long n, const void* a, const void* b, double* out)
+{
+  if (csem_device_count() < 1) return csem_set_error(CSEM_ENODEV, "no CUDA device available");
+  typedef typename P::C C;
+  DevBuf A, B, part, res;
+  const int nblk = dot_blocks(n);
+  A.alloc(sizeof(C) * (size_t)(n > 0 ? n : 1));
+  B.alloc(sizeof(C) * (size_t)(n > 0 ? n : 1));
+  part.alloc(sizeof(double2) * nblk);
+  res.alloc(sizeof(double2));
+  CSEM_CUDA_TRY(cudaMemcpy(A.p, a, sizeof(C) * (size_t)n, cudaMemcpyHostToDevice));
+  CSEM_CUDA_TRY(cudaMemcpy(B.p, b, sizeof(C) * (size_t)n, cudaMemcpyHostToDevice));
+  launch_dot<P>(A.as<C>(), B.as<C>(), n, n, 1, nullptr, part.as<double2>(), nblk, res.as<double2>(), 0);
+  CSEM_CUDA_TRY(cudaGetLastError());
+  CSEM_CUDA_TRY(cudaMemcpy(out, res.p, sizeof(double2), cudaMemcpyDeviceToHost));
+  return CSEM_OK;
+}
+
+extern "C" {
+
+int csem_fdfd_apply_host(csem_ctx* c, double re, double im, const double* x, double* y)
+{
+  API_BEGIN return op_host<F64>(c, OP_A, re, im, x, y); API_END
+}
+int csem_lusgs_apply_host(csem_ctx* c, double re, double im, const double* x, double* y)
+{
+  API_BEGIN return op_host<F64>(c, OP_LUSGS, re, im, x, y); API_END
+}
+int csem_aphi_apply_host(csem_ctx* c, double re, double im, const double* x, double* y)
+{
+  API_BEGIN return op_host<F64>(c, OP_APHI, re, im, x, y); API_END
+}
+int csem_fdfd_apply_c64_host(csem_ctx* c, double re, double im, const float* x, float* y)
+{
+  API_BEGIN return op_host<F32>(c, OP_A, re, im, x, y); API_END
+}
+int csem_lusgs_apply_c64_host(csem_ctx* c, double re, double im, const float* x, float* y)
+{
+  API_BEGIN return op_host<F32>(c, OP_LUSGS, re, im, x, y); API_END
+}
+int csem_aphi_apply_c64_host(csem_ctx* c, double re, double im, const float* x, float* y)
+{
+  API_BEGIN return op_host<F32>(c, OP_APHI, re, im, x, y); API_END
+}
+
+static Solver64* solver_for(csem_ctx* c)
+{
+  if (!c->solver) c->solver = new Solver64(c->model, c->st);
+  return c->solver;
+}
+
+int csem_gmres_pre_apply_host(csem_ctx* c, double re, double im, int mp, const double* x, double* y)
+{
+  if (mp < 1) return csem_set_error(CSEM_EINVAL, "mp must be >= 1");
+  API_BEGIN
+  Solver64* s = solver_for(c);
+  const size_t bytes = sizeof(double2) * (size_t)c->model->lE;
+  ensure(c->io[0], bytes);
+  ensure(c->io[1], bytes);
+  s->set_iom(re, im);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[0].p, x, bytes, cudaMemcpyHostToDevice, c->st));
+  s->gmres_pre(mp, c->io[0].as<double2>(), c->io[1].as<double2>());
+  CSEM_CUDA_TRY(cudaMemcpyAsync(y, c->io[1].p, bytes, cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  API_END
+}
+
+int csem_airbc_apply_host(csem_ctx* c, const double* hz0, double* hx, double* hy)
+{
+  Model* m = c->model;
+  if (!m->airbc) return csem_set_error(CSEM_EINVAL, "context was created with airbc=0");
+  API_BEGIN
+  Ops<F64>* o = ops64_for(c, 1);
+  const size_t nz = sizeof(double2) * (size_t)m->n1 * m->n2;
+  CSEM_CUDA_TRY(cudaMemcpyAsync(o->hz0.p, hz0, nz, cudaMemcpyHostToDevice, c->st));
+  const AirP<F64>& a = m->a64;
+  launch_air_gather<F64>(a, o->hz0.as<double2>(), o->K.as<double2>(), 1, c->st);
+  o->fft->exec(true, o->K.p, 1, CUFFT_FORWARD, c->st);
+  launch_air_filter<F64>(a, o->K.as<double2>(), o->K2.as<double2>(), 1, c->st);
+  o->fft->exec(true, o->K2.p, 2, CUFFT_INVERSE, c->st);
+  launch_air_scatter<F64>(a, o->K2.as<double2>(), o->ghx.as<double2>(), o->ghy.as<double2>(), 1, c->st);
+  CSEM_CUDA_TRY(cudaGetLastError());
+  CSEM_CUDA_TRY(cudaMemcpyAsync(hx, o->ghx.p, sizeof(double2) * (size_t)(m->n1 + 1) * m->n2, cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaMemcpyAsync(hy, o->ghy.p, sizeof(double2) * (size_t)m->n1 * (m->n2 + 1), cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  API_END
+}
+
+// ---------------------------------------------------------------- dots
+int csem_cdot_host(long n, const double* a, const double* b, double* out)
+{
+  API_BEGIN return cdot_host<F64>(n, a, b, out); API_END
+}
+int csem_cdot_c64_host(long n, const float* a, const float* b, double* out)
+{
+  API_BEGIN return cdot_host<F32>(n, a, b, out); API_END
+}
+
+// ---------------------------------------------------------------- inject / extract
+int csem_inject_host(csem_ctx* c, double re, double im, int nch, const int* ch, const float* src3, double* b)
+{
+  API_BEGIN
+  Model* m = c->model;
+  const size_t bytes = sizeof(double2) * (size_t)m->lE;
+  ensure(c->io[0], bytes);
+  ensure(c->io[2], 64 + sizeof(int) * 8);
+  double2 iom = make_double2(re, im);
+  char stage[64 + sizeof(int) * 8];
+  memcpy(stage, src3, sizeof(float) * 3);
+  memcpy(stage + 16, &iom, sizeof(iom));
+  int nc = nch > 8 ? 8 : nch;
+  memcpy(stage + 64, ch, sizeof(int) * nc);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[2].p, stage, sizeof(stage), cudaMemcpyHostToDevice, c->st));
+  CSEM_CUDA_TRY(cudaMemsetAsync(c->io[0].p, 0, bytes, c->st));
+  char* d = c->io[2].as<char>();
+  launch_inject(m->acq, 1, (const float*)d, (const double2*)(d + 16), (const int*)(d + 64), nc, c->io[0].as<double2>(), c->st);
+  CSEM_CUDA_TRY(cudaGetLastError());
+  CSEM_CUDA_TRY(cudaMemcpyAsync(b, c->io[0].p, bytes, cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  API_END
+}
+
+int csem_extract_host(csem_ctx* c, int nch, const int* ch, int nrec, const float* rec, const double* x, double* out)
+{
+  API_BEGIN
+  Model* m = c->model;
+  const size_t bytes = sizeof(double2) * (size_t)m->lE;
+  ensure(c->io[0], bytes);
+  const size_t rb = sizeof(float) * 5 * (size_t)nrec, cb = sizeof(int) * nch, ob = sizeof(double2) * (size_t)nch * nrec;
+  ensure(c->io[2], rb + cb + 16);
+  ensure(c->io[3], ob + 16);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[0].p, x, bytes, cudaMemcpyHostToDevice, c->st));
+  char* d = c->io[2].as<char>();
+  CSEM_CUDA_TRY(cudaMemcpyAsync(d, rec, rb, cudaMemcpyHostToDevice, c->st));
+  CSEM_CUDA_TRY(cudaMemcpyAsync(d + rb, ch, cb, cudaMemcpyHostToDevice, c->st));
+  launch_extract<double2>(m->acq, 1, nch, (const int*)(d + rb), nrec, (const float*)d, c->io[0].as<double2>(), m->lE,
+                          nullptr, c->io[3].as<double2>(), c->st);
+  CSEM_CUDA_TRY(cudaGetLastError());
+  CSEM_CUDA_TRY(cudaMemcpyAsync(out, c->io[3].p, ob, cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  API_END
+}
+
+// ---------------------------------------------------------------- FP64 solve
+int csem_solve_fp64_host(csem_ctx* c, int algopt, int preco, int niter, double tol, int nrestart, int mp,
+                         double re, double im, const double* b, double* x, double* hist, int hist_cap, int* nhist,
+                         int* iters, int* status)
+{
+  if (algopt != 1 && algopt != 2) return csem_set_error(CSEM_EINVAL, "algopt must be 1 (BiCGStab) or 2 (GMRES)");
+  if (preco < 0 || preco > 3) return csem_set_error(CSEM_EINVAL, "preco must be 0..3");
+  if (algopt == 2 && nrestart < 1) return csem_set_error(CSEM_EINVAL, "nrestart must be >= 1");
+  if (preco == 2 && mp < 1) return csem_set_error(CSEM_EINVAL, "mp must be >= 1");
+  API_BEGIN
+  Solver64* s = solver_for(c);
+  const size_t bytes = sizeof(double2) * (size_t)c->model->lE;
+  ensure(c->io[0], bytes);
+  ensure(c->io[1], bytes);
+  s->set_iom(re, im);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[0].p, b, bytes, cudaMemcpyHostToDevice, c->st));
+  CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[1].p, x, bytes, cudaMemcpyHostToDevice, c->st));
+  std::vector<double> h;
+  int st = ST_RUNNING, it;
+  if (algopt == 1)
+    it = s->fbicgstab(preco, mp, c->io[1].as<double2>(), c->io[0].as<double2>(), niter, tol, h, st, preco != 0);
+  else
+    it = s->gmres(preco, mp, c->io[1].as<double2>(), c->io[0].as<double2>(), niter / nrestart, tol, nrestart, h, st);
+  CSEM_CUDA_TRY(cudaGetLastError());
+  CSEM_CUDA_TRY(cudaMemcpyAsync(x, c->io[1].p, bytes, cudaMemcpyDeviceToHost, c->st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  if (hist)
+    for (int q = 0; q < (int)h.size() && q < hist_cap; q++) hist[q] = h[q];
+  if (nhist) *nhist = (int)h.size();
+  if (iters) *iters = it;
+  if (status) *status = st;
+  API_END
+}
+
+// ---------------------------------------------------------------- device pointers
+static int op_dev(csem_ctx* c, int which, int prec, int nsys, const double* iom, const void* x, void* y, void* stream)
+{
+  if (prec != 64 && prec != 32) return csem_set_error(CSEM_EINVAL, "prec must be 64 or 32");
+  if (nsys < 1) return csem_set_error(CSEM_EINVAL, "nsys must be >= 1");
+  upload_scal(c, nsys, iom);
+  cudaStream_t user = (cudaStream_t)stream;
+  if (user) {  // order after the caller's work
+    cudaEvent_t ev;
+    CSEM_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CSEM_CUDA_TRY(cudaEventRecord(ev, user));
+    CSEM_CUDA_TRY(cudaStreamWaitEvent(c->st, ev, 0));
+    cudaEventDestroy(ev);
+  }
+  if (prec == 64) {
+    Ops<F64>* o = ops64_for(c, nsys);
+    const SysScal<F64>* s = c->sc64.as<SysScal<F64>>();
+    if (which == OP_A) o->apply_A((const double2*)x, (double2*)y, nsys, nullptr, s);
+    else if (which == OP_LUSGS) o->apply_lusgs((const double2*)x, (double2*)y, nsys, nullptr, s);
+    else o->apply_aphi((const double2*)x, (double2*)y, nsys, nullptr, s);
+  } else {
+    Ops<F32>* o = ops32_for(c, nsys);
+    const SysScal<F32>* s = c->sc32.as<SysScal<F32>>();
+    if (which == OP_A) o->apply_A((const float2*)x, (float2*)y, nsys, nullptr, s);
+    else if (which == OP_LUSGS) o->apply_lusgs((const float2*)x, (float2*)y, nsys, nullptr, s);
+    else o->apply_aphi((const float2*)x, (float2*)y, nsys, nullptr, s);
+  }
+  CSEM_CUDA_TRY(cudaGetLastError());
+  if (user) {
+    cudaEvent_t ev;
+    CSEM_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CSEM_CUDA_TRY(cudaEventRecord(ev, c->st));
+    CSEM_CUDA_TRY(cudaStreamWaitEvent(user, ev, 0));
+    cudaEventDestroy(ev);
+  }
+  return CSEM_OK;
+}
+
+int csem_fdfd_apply_dev(csem_ctx* c, int prec, int nsys, const double* iom, const void* x, void* y, void* stream)
+{
+  API_BEGIN return op_dev(c, OP_A, prec, nsys, iom, x, y, stream); API_END
+}
+int csem_lusgs_apply_dev(csem_ctx* c, int prec, int nsys, const double* iom, const void* x, void* y, void* stream)
+{
+  API_BEGIN return op_dev(c, OP_LUSGS, prec, nsys, iom, x, y, stream); API_END
+}
+int csem_aphi_apply_dev(csem_ctx* c, int prec, int nsys, const double* iom, const void* x, void* y, void* stream)
+{
+  API_BEGIN return op_dev(c, OP_APHI, prec, nsys, iom, x, y, stream); API_END
+}
+
+int csem_cdot_dev(int prec, long n, int nsys, const void* a, const void* b, double* out_dev, void* stream)
+{
+  if (prec != 64 && prec != 32) return csem_set_error(CSEM_EINVAL, "prec must be 64 or 32");
+  API_BEGIN
+  const int nblk = dot_blocks(n);
+  static DevBuf part;
+  ensure(part, sizeof(double2) * (size_t)nblk * nsys);
+  if (prec == 64)
+    launch_dot<F64>((const double2*)a, (const double2*)b, n, n, nsys, nullptr, part.as<double2>(), nblk,
+                    (double2*)out_dev, (cudaStream_t)stream);
+  else
+    launch_dot<F32>((const float2*)a, (const float2*)b, n, n, nsys, nullptr, part.as<double2>(), nblk,
+                    (double2*)out_dev, (cudaStream_t)stream);
+  CSEM_CUDA_TRY(cudaGetLastError());
+  API_END
+}
+
+}  // extern "C"

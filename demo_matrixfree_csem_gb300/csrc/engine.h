@@ -1,0 +1,82 @@
+// Internal C++ interface between the kernel files and the solver engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include "csem_cuda.cuh"
+
+namespace csem {
+
+// ---------------------------------------------------------------- operator
+template <class P>
+void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
+                 const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
+                 cudaStream_t st);
+template <class P>
+void launch_hz0(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* out,
+                int nsys, const int* sys_list, cudaStream_t st);
+
+// ---------------------------------------------------------------- airwave
+// Tables of airbc_init_free.c:86-105 and of the back-interpolation
+// (airbc_init_free.c:168-207), precomputed on the host in double.
+template <class P> struct AirP {
+  typedef typename P::R R;
+  int n1, n2, N1, N2;
+  const int *jx, *jy;      // gather cell per uniform node, -1 outside x1s[n1-1] / x2s[n2-1]
+  const R *wx, *wy;
+  const int *hx_j1, *hx_j2;  // Hx ghost: per i1 <= n1 (from x1), per i2 < n2 (from x2s)
+  const R *hx_w1, *hx_w2;
+  const int *hy_j1, *hy_j2;  // Hy ghost: per i1 < n1 (from x1s), per i2 <= n2 (from x2)
+  const R *hy_w1, *hy_w2;
+  const typename P::C *sH1, *sH2;  // [N2][N1]
+};
+
+template <class P>
+void launch_air_gather(const AirP<P>& a, const typename P::C* hz0, typename P::C* K, int nslot, cudaStream_t st);
+template <class P>
+void launch_air_filter(const AirP<P>& a, const typename P::C* K, typename P::C* K2, int nslot, cudaStream_t st);
+template <class P>
+void launch_air_scatter(const AirP<P>& a, const typename P::C* K2, typename P::C* ghx, typename P::C* ghy,
+                        int nslot, cudaStream_t st);
+
+// ---------------------------------------------------------------- LU-SGS / A-phi
+// A component sweep over one wavefront diagonal. The sweep grid has nK planes
+// (full grid for LU-SGS with airbc); stored vector plane = sweep plane - vshift,
+// planes below vshift live in the cap scratch (air layers).
+template <class P> struct SweepP {
+  GridP<P> g;          // d3/sigma pointers already shifted by dshift
+  int nK;              // sweep grid depth
+  int vshift;          // planes below vshift are air (cap)
+  const typename P::C* X;   // right-hand side (operator grid), [sys][lE]
+  typename P::C* Y;         // solution (operator grid), [sys][lE]
+  typename P::C* CAP;       // [slot][capE] air planes, full-grid plane layout
+  long capEx, capEy, capE;  // cap component offsets
+  const SysScal<P>* scal;
+  const int* sys_list;
+  // A-phi only
+  const typename P::C* V;   // node potential [slot][lv]
+  const typename P::R *s11u, *s22u, *s33u;  // unshifted full-grid sigma (the Q2 lookups)
+  const typename P::C* BV;  // divergence right-hand side [slot][lv]
+  long lv;
+};
+
+template <class P>
+void launch_lusgs_zero_bounds(const SweepP<P>& s, int nslot, cudaStream_t st);
+template <class P>
+void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int nslot, cudaStream_t st);
+int sweep_diagonals(int comp, int n1, int n2, int nK);  // number of diagonals t (2..)
+
+template <class P>
+void launch_aphi_div(const SweepP<P>& s, typename P::C* BV, int nslot, cudaStream_t st);
+template <class P>
+void launch_aphi_phi(const SweepP<P>& s, typename P::C* V, int t, int nslot, cudaStream_t st);
+int phi_diagonals(int n1, int n2, int n3);
+template <class P>
+void launch_aphi_grad(const SweepP<P>& s, const typename P::C* V, int nslot, cudaStream_t st);
+
+// ---------------------------------------------------------------- BLAS-1
+template <class P>
+void launch_dot(const typename P::C* a, const typename P::C* b, long n, long stride, int nslot,
+                const int* sys_list, double2* partial, int nblk, double2* out, cudaStream_t st);
+int dot_blocks(long n);
+
+}  // namespace csem

@@ -1,0 +1,97 @@
+// Device-resident model and the operator / preconditioner applications built on it.
+#pragma once
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <vector>
+#include "csem_cuda.cuh"
+#include "engine.h"
+#include "engine_acq.h"
+#include "solver_state.h"
+
+struct csem_grid;
+
+namespace csem {
+
+#define CSEM_CUDA_TRY(x)                                                     \
+  do {                                                                       \
+    cudaError_t e_ = (x);                                                    \
+    if (e_ != cudaSuccess) throw CudaError(e_, #x, __FILE__, __LINE__);      \
+  } while (0)
+
+struct CudaError {
+  cudaError_t err;
+  const char *expr, *file;
+  int line;
+  CudaError(cudaError_t e, const char* x, const char* f, int l) : err(e), expr(x), file(f), line(l) {}
+};
+struct CsemError {
+  int code;
+  char msg[256];
+};
+
+// device allocation owned by a Model / workspace
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void alloc(size_t b);
+  void free_();
+  ~DevBuf() { free_(); }
+  template <class T> T* as() const { return (T*)p; }
+};
+
+enum Precond { PRE_NONE = 0, PRE_LUSGS = 1, PRE_GMRES = 2, PRE_APHI = 3 };
+
+// FFT plans for batches of 1,2,4,..,2^k uniform airwave grids
+struct FftPlans {
+  int N1 = 0, N2 = 0;
+  std::vector<cufftHandle> z, c;  // index = log2(batch)
+  ~FftPlans();
+  void exec(bool dbl, void* data, int count, int dir, cudaStream_t st);
+};
+
+class Model {
+ public:
+  Model(const csem_grid* g, int airbc, int fvm);
+  ~Model();
+  // geometry
+  int n1, n2, n3, n3f, nb, nz, airbc, fvm;
+  long lEx, lEy, lEz, lE, lv;
+  float rho_water;
+  int N1 = 0, N2 = 0;  // airwave grid
+  // device data
+  DevBuf d64, d32, s64, s32, x64, air_i, air_w64, air_w32, sH64, sH32;
+  GridP<F64> g64;  // operator view (kstart shift applied inside kernels)
+  GridP<F32> g32;
+  AirP<F64> a64;
+  AirP<F32> a32;
+  AcqGrid acq;
+  template <class P> const GridP<P>& grid() const;
+  template <class P> const AirP<P>& air() const;
+  template <class P> GridP<P> grid_shifted() const;  // d3/sigma advanced by kstart planes
+};
+
+// Per-precision workspace for nslot systems on one model.
+template <class P>
+class Ops {
+ public:
+  typedef typename P::C C;
+  Ops(Model* m, int nslot_max, cudaStream_t st);
+  Model* m;
+  int nmax;
+  cudaStream_t st;
+  DevBuf hz0, K, K2, ghx, ghy, cap, V, BV, scal;
+  FftPlans* fft;
+  // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal)
+  void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
+  void apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
+  void apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
+  void zero(C* Y, long n, int nslot, const int* sys_list);
+  ~Ops();
+};
+
+FftPlans* fft_plans_for(int N1, int N2);
+
+SysScal<F64> sys_scal64(double iom_re, double iom_im);
+SysScal<F32> sys_scal32(const SysScal<F64>& s);
+
+}  // namespace csem

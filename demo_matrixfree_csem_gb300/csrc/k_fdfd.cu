@@ -1,0 +1,184 @@
+// y = A x: the staggered-grid curl-curl operator of fdfd_apply (fdfd.c:86-205).
+//
+// One CTA owns a BX x BY tile of (i,j) columns plus a one-column halo on the low side
+// (the halo threads only compute H) and marches a chunk of z-planes. At each plane it
+// computes H = curl E / (i omega mu0) for its columns (fdfd.c:125-149), shares it through
+// shared memory, and produces y = curl H - sigma E for the tile (fdfd.c:176-203). H is
+// never written to HBM, so one pass reads x and sigma and writes y.
+//
+// With the airwave boundary (airbc=1) the k=0 rows of bx/by use the ghost fields
+// Hx(z=-dz/2), Hy(z=-dz/2) that the airwave pipeline derives from Hz(z=0)
+// (fdfd.c:151-172); k_hz0 provides that Hz plane.
+#include "csem_cuda.cuh"
+#include "engine.h"
+
+namespace csem {
+
+template <class P>
+__device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __restrict__ Ex,
+                                     const typename P::C* __restrict__ Ey, const typename P::C* __restrict__ Ez,
+                                     typename P::C iwmu, int k, int j, int i, typename P::C& hx,
+                                     typename P::C& hy, typename P::C& hz)
+{
+  typedef typename P::C C;
+  const int n1 = g.n1, n2 = g.n2, n3 = g.n3, kf = k + g.kstart;
+  hx = hy = hz = czero<P>();
+  if (i < 0 || j < 0 || i > n1 || j > n2) return;
+  if (j < n2 && k < n3) {  // Hx = (dEz/dy - dEy/dz) / (i w mu0)
+    C t1 = cdivs<P>(csub<P>(Ez[ix3(n1, n2, k, j + 1, i)], Ez[ix3(n1, n2, k, j, i)]), g.d2s[j], g.r2s[j]);
+    C t2 = cdivs<P>(csub<P>(Ey[ix2(n1, n2, k + 1, j, i)], Ey[ix2(n1, n2, k, j, i)]), g.d3s[kf], g.r3s[kf]);
+    hx = cmul<P>(csub<P>(t1, t2), iwmu);
+  }
+  if (i < n1 && k < n3) {  // Hy = (dEx/dz - dEz/dx) / (i w mu0)
+    C t1 = cdivs<P>(csub<P>(Ex[ix1(n1, n2, k + 1, j, i)], Ex[ix1(n1, n2, k, j, i)]), g.d3s[kf], g.r3s[kf]);
+    C t2 = cdivs<P>(csub<P>(Ez[ix3(n1, n2, k, j, i + 1)], Ez[ix3(n1, n2, k, j, i)]), g.d1s[i], g.r1s[i]);
+    hy = cmul<P>(csub<P>(t1, t2), iwmu);
+  }
+  if (i < n1 && j < n2) {  // Hz = (dEy/dx - dEx/dy) / (i w mu0)
+    C t1 = cdivs<P>(csub<P>(Ey[ix2(n1, n2, k, j, i + 1)], Ey[ix2(n1, n2, k, j, i)]), g.d1s[i], g.r1s[i]);
+    C t2 = cdivs<P>(csub<P>(Ex[ix1(n1, n2, k, j + 1, i)], Ex[ix1(n1, n2, k, j, i)]), g.d2s[j], g.r2s[j]);
+    hz = cmul<P>(csub<P>(t1, t2), iwmu);
+  }
+}
+
+template <class P, int BX, int BY>
+__global__ void __launch_bounds__((BX + 1) * (BY + 1))
+k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
+       typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
+       const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list)
+{
+  typedef typename P::C C;
+  typedef typename P::R R;
+  __shared__ C sHx[BY + 1][BX + 1], sHy[BY + 1][BX + 1], sHz[BY + 1][BX + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * BX + tx - 1;
+  const int j = blockIdx.y * BY + ty - 1;
+  const int slot = blockIdx.z / nkc, kc = blockIdx.z % nkc;
+  const int sys = sys_list ? sys_list[slot] : slot;
+  const int n1 = g.n1, n2 = g.n2, n3 = g.n3, ks = g.kstart;
+  const C* Ex = X + (size_t)sys * g.lE;
+  const C* Ey = Ex + g.lEx;
+  const C* Ez = Ey + g.lEy;
+  C* bx = Y + (size_t)sys * g.lE;
+  C* by = bx + g.lEx;
+  C* bz = by + g.lEy;
+  const C iwmu = scal[sys].iwmu, iom = scal[sys].iom;
+  const C* ghx = GHX ? GHX + (size_t)slot * (n1 + 1) * n2 : nullptr;  // ghosts are per slot
+  const C* ghy = GHY ? GHY + (size_t)slot * n1 * (n2 + 1) : nullptr;
+  const int kb = kc * kchunk;
+  const int ke = min(n3 + 1, kb + kchunk);
+  const bool interior = tx >= 1 && ty >= 1 && i <= n1 && j <= n2;
+
+  C pHx = czero<P>(), pHy = czero<P>(), hx, hy, hz;
+  if (kb > 0) {
+    h_at<P>(g, Ex, Ey, Ez, iwmu, kb - 1, j, i, hx, hy, hz);
+    pHx = hx;
+    pHy = hy;
+  }
+  for (int k = kb; k < ke; k++) {
+    h_at<P>(g, Ex, Ey, Ez, iwmu, k, j, i, hx, hy, hz);
+    sHx[ty][tx] = hx;
+    sHy[ty][tx] = hy;
+    sHz[ty][tx] = hz;
+    __syncthreads();
+    if (interior) {
+      const int kf = k + ks;
+      if (i < n1) {  // bx
+        C r = czero<P>();
+        const bool in = j >= 1 && j <= n2 - 1 && ((k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc));
+        if (in) {
+          C hyb = k >= 1 ? pHy : ghy[i + (long)n1 * j];
+          C t1 = cdivs<P>(csub<P>(hz, sHz[ty - 1][tx]), g.d2[j], g.r2[j]);
+          C t2 = cdivs<P>(csub<P>(hy, hyb), g.d3[kf], g.r3[kf]);
+          long p = ix1(n1, n2, k, j, i);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s11[ix1(n1, n2, kf, j, i)], Ex[p]));
+          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[kf]), iom));
+        }
+        bx[ix1(n1, n2, k, j, i)] = r;
+      }
+      if (j < n2) {  // by
+        C r = czero<P>();
+        const bool in = i >= 1 && i <= n1 - 1 && ((k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc));
+        if (in) {
+          C hxb = k >= 1 ? pHx : ghx[i + (long)(n1 + 1) * j];
+          C t1 = cdivs<P>(csub<P>(hx, hxb), g.d3[kf], g.r3[kf]);
+          C t2 = cdivs<P>(csub<P>(hz, sHz[ty][tx - 1]), g.d1[i], g.r1[i]);
+          long p = ix2(n1, n2, k, j, i);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s22[ix2(n1, n2, kf, j, i)], Ey[p]));
+          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1[i], g.d2s[j]), g.d3[kf]), iom));
+        }
+        by[ix2(n1, n2, k, j, i)] = r;
+      }
+      if (k < n3) {  // bz
+        C r = czero<P>();
+        if (i >= 1 && i <= n1 - 1 && j >= 1 && j <= n2 - 1) {
+          C t1 = cdivs<P>(csub<P>(hy, sHy[ty][tx - 1]), g.d1[i], g.r1[i]);
+          C t2 = cdivs<P>(csub<P>(hx, sHx[ty - 1][tx]), g.d2[j], g.r2[j]);
+          long p = ix3(n1, n2, k, j, i);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s33[ix3(n1, n2, kf, j, i)], Ez[p]));
+          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1[i], g.d2[j]), g.d3s[kf]), iom));
+        }
+        bz[ix3(n1, n2, k, j, i)] = r;
+      }
+    }
+    pHx = hx;
+    pHy = hy;
+    __syncthreads();
+  }
+  (void)sizeof(R);
+}
+
+// Hz on the plane k=0 (operator grid) for the airwave: out[sys][j][i], i<n1, j<n2
+template <class P>
+__global__ void k_hz0(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
+                      typename P::C* __restrict__ out, const int* __restrict__ sys_list)
+{
+  const int slot = blockIdx.z;
+  const int sys = sys_list ? sys_list[slot] : slot;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n1 || j >= g.n2) return;
+  const typename P::C* Ex = X + (size_t)sys * g.lE;
+  const typename P::C* Ey = Ex + g.lEx;
+  const typename P::C* Ez = Ey + g.lEy;
+  typename P::C hx, hy, hz;
+  h_at<P>(g, Ex, Ey, Ez, scal[sys].iwmu, 0, j, i, hx, hy, hz);
+  out[(size_t)slot * g.n1 * g.n2 + i + (long)g.n1 * j] = hz;
+}
+
+template <class P>
+void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
+                 const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
+                 cudaStream_t st)
+{
+  constexpr int BX = 32, BY = 8;
+  dim3 blk(BX + 1, BY + 1);
+  int gx = (g.n1 + 1 + BX - 1) / BX, gy = (g.n2 + 1 + BY - 1) / BY;
+  long base = (long)gx * gy * nsys;
+  int nkc = (int)((4L * 152 + base - 1) / base);
+  if (nkc < 1) nkc = 1;
+  if (nkc > (g.n3 + 1) / 4) nkc = (g.n3 + 1) / 4 > 0 ? (g.n3 + 1) / 4 : 1;
+  int kchunk = (g.n3 + 1 + nkc - 1) / nkc;
+  nkc = (g.n3 + 1 + kchunk - 1) / kchunk;
+  dim3 grd(gx, gy, nsys * nkc);
+  k_fdfd<P, BX, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
+}
+
+template <class P>
+void launch_hz0(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* out,
+                int nsys, const int* sys_list, cudaStream_t st)
+{
+  dim3 blk(32, 8);
+  dim3 grd((g.n1 + 31) / 32, (g.n2 + 7) / 8, nsys);
+  k_hz0<P><<<grd, blk, 0, st>>>(g, scal, X, out, sys_list);
+}
+
+template void launch_fdfd<F64>(const GridP<F64>&, const SysScal<F64>*, const double2*, double2*,
+                               const double2*, const double2*, int, const int*, cudaStream_t);
+template void launch_fdfd<F32>(const GridP<F32>&, const SysScal<F32>*, const float2*, float2*,
+                               const float2*, const float2*, int, const int*, cudaStream_t);
+template void launch_hz0<F64>(const GridP<F64>&, const SysScal<F64>*, const double2*, double2*, int,
+                              const int*, cudaStream_t);
+template void launch_hz0<F32>(const GridP<F32>&, const SysScal<F32>*, const float2*, float2*, int,
+                              const int*, cudaStream_t);
+
+}  // namespace csem

@@ -210,22 +210,22 @@ int csem_grid_extend(csem_grid_t *g, int nb, float lextend, float rho_air, int i
   if (nb > 0) {
     double len = g->lextend, r;
     dx = x1n[1] - x1n[0];
-    r = g->rstretch[0] = nugrid_ratio(nb, len, dx, istretch);
+    r = g->rstretch[0] = (float)nugrid_ratio(nb, len, dx, istretch); /* emf->rstretch is a float */
     for (int i = 0; i < nb; i++) g->x1[nb - 1 - i] = g->x1[nb - i] - dx * pow(r, i);
     dx = x1n[nx] - x1n[nx - 1];
-    r = g->rstretch[1] = nugrid_ratio(nb, len, dx, istretch);
+    r = g->rstretch[1] = (float)nugrid_ratio(nb, len, dx, istretch); /* emf->rstretch is a float */
     for (int i = 0; i < nb; i++) g->x1[nb + nx + 1 + i] = g->x1[nb + nx + i] + dx * pow(r, i);
     dx = x2n[1] - x2n[0];
-    r = g->rstretch[2] = nugrid_ratio(nb, len, dx, istretch);
+    r = g->rstretch[2] = (float)nugrid_ratio(nb, len, dx, istretch); /* emf->rstretch is a float */
     for (int j = 0; j < nb; j++) g->x2[nb - 1 - j] = g->x2[nb - j] - dx * pow(r, j);
     dx = x2n[ny] - x2n[ny - 1];
-    r = g->rstretch[3] = nugrid_ratio(nb, len, dx, istretch);
+    r = g->rstretch[3] = (float)nugrid_ratio(nb, len, dx, istretch); /* emf->rstretch is a float */
     for (int j = 0; j < nb; j++) g->x2[nb + ny + 1 + j] = g->x2[nb + ny + j] + dx * pow(r, j);
     dx = x3n[1] - x3n[0];
-    r = g->rstretch[4] = nugrid_ratio(nb, len, dx, istretch);
+    r = g->rstretch[4] = (float)nugrid_ratio(nb, len, dx, istretch); /* emf->rstretch is a float */
     for (int k = 0; k < nb; k++) g->x3[nb - 1 - k] = g->x3[nb - k] - dx * pow(r, k);
     dx = x3n[nz] - x3n[nz - 1];
-    r = g->rstretch[5] = nugrid_ratio(nb, len, dx, istretch);
+    r = g->rstretch[5] = (float)nugrid_ratio(nb, len, dx, istretch); /* emf->rstretch is a float */
     for (int k = 0; k < nb; k++) g->x3[nb + nz + 1 + k] = g->x3[nb + nz + k] + dx * pow(r, k);
   }
   staggered(n1, g->x1, g->x1s, g->d1, g->d1s);

@@ -1,0 +1,113 @@
+/* csem_gpu.h - C ABI of the GB300 CSEM solver (libcsem_gpu.so).
+ *
+ * The reference's hot path is a set of C callbacks over a global model
+ * (op_t = void (*)(int, complex*, complex*), solver.h:4; emf set by fdfd_init,
+ * fdfd.c:23,30-63). This library replaces it with a handle (csem_ctx) that owns one
+ * padded model resident in GPU memory, a CUDA stream and workspaces, plus entry points
+ * that take plain pointers and sizes.
+ *
+ * Conventions
+ *  - complex128 vectors are interleaved doubles (re, im), complex64 interleaved floats,
+ *    in the reference's layout E = [Ex | Ey | Ez] with Ex(k,j,i) at i + n1*(j+(n2+1)*k),
+ *    Ey at i + (n1+1)*(j+n2*k), Ez at i + (n1+1)*(j+(n2+1)*k) (fdfd.c:13-15), on the
+ *    operator grid (n3 = nz+nb with airbc=1, else nz+2nb);
+ *  - "_host" buffers live in host memory (copied in and out inside the call); "_dev"
+ *    buffers are device pointers and `stream` is a cudaStream_t (NULL: the context's);
+ *  - every function returns CSEM_OK (0) or a negative CSEM_E* code (csem_host.h) and
+ *    leaves a message in csem_last_error(); nothing exits the process;
+ *  - iom = I*omega*mu0 = (0, 2*pi*f*mu0) as the reference's driver sets it (main.c:95).
+ * The FP64 entry points reproduce the reference's arithmetic bit for bit except for the
+ * summation order inside dot products (deterministic, fixed tree).
+ */
+#ifndef CSEM_GPU_H
+#define CSEM_GPU_H
+#include "csem_host.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct csem_ctx csem_ctx;
+
+const char *csem_version(void);
+/* number of visible CUDA devices (0 without a GPU; never fails) */
+int csem_device_count(void);
+
+/* Upload a padded model (csem_grid_extend / csem_grid_airbc done) for the operator
+ * with airbc/fvm. Replaces fdfd_init (fdfd.c:30-63) and airbc_init
+ * (airbc_init_free.c:24-109) state. */
+int csem_ctx_create(const csem_grid_t *g, int airbc, int fvm, csem_ctx **out);
+/* Replaces fdfd_free (fdfd.c:65-80) / airbc_free (airbc_init_free.c:111-124). */
+void csem_ctx_destroy(csem_ctx *c);
+/* [lE, lEx, lEy, lEz, lv, n1, n2, n3(operator), n3 full, nb] */
+int csem_ctx_sizes(const csem_ctx *c, long *out10);
+
+/* ------------------------------------------------------------ operators (FP64)
+ * y = A x. Replaces fdfd_apply (fdfd.c:86-205). */
+int csem_fdfd_apply_host(csem_ctx *c, double iom_re, double iom_im, const double *x, double *y);
+/* y = M^-1 x, LU-SGS. Replaces lusgs_apply (fdfd.c:287-510). */
+int csem_lusgs_apply_host(csem_ctx *c, double iom_re, double iom_im, const double *x, double *y);
+/* y = M^-1 x, A-phi. Replaces aphi_apply (fdfd.c:513-821). */
+int csem_aphi_apply_host(csem_ctx *c, double iom_re, double iom_im, const double *x, double *y);
+/* y = M^-1 x, mp steps of GMRES on A. Replaces gmres_apply (gmres_init_free.c:58-137). */
+int csem_gmres_pre_apply_host(csem_ctx *c, double iom_re, double iom_im, int mp, const double *x, double *y);
+/* Airwave ghosts from Hz(z=0) [n2][n1] -> Hx [n2][n1+1], Hy [n2+1][n1].
+ * Replaces airbc_apply (airbc_init_free.c:130-209). */
+int csem_airbc_apply_host(csem_ctx *c, const double *hz0, double *hx, double *hy);
+
+/* ------------------------------------------------------------ operators (complex64)
+ * The same operators in complex64, as the mixed-precision inner solver runs them. */
+int csem_fdfd_apply_c64_host(csem_ctx *c, double iom_re, double iom_im, const float *x, float *y);
+int csem_lusgs_apply_c64_host(csem_ctx *c, double iom_re, double iom_im, const float *x, float *y);
+int csem_aphi_apply_c64_host(csem_ctx *c, double iom_re, double iom_im, const float *x, float *y);
+
+/* ------------------------------------------------------------ dot products
+ * out = sum a_i conj(b_i). Replaces cdotprod (cdotprod.c:13-19). */
+int csem_cdot_host(long n, const double *a, const double *b, double *out2);
+int csem_cdot_c64_host(long n, const float *a, const float *b, double *out2);
+
+/* ------------------------------------------------------------ source / receivers
+ * b = unit dipole(s) at src = (x1,x2,x3) for channels ch[] (0 Ex, 1 Ey, 2 Ez); b is
+ * zeroed first. Replaces inject_source (inject_extract.c:24-120). */
+int csem_inject_host(csem_ctx *c, double iom_re, double iom_im, int nch, const int *ch, const float *src3,
+                     double *b);
+/* out[ic][r] (complex128) = receiver r of channel ch[ic]; rec is [nrec][5] rows
+ * (x1 x2 x3 azimuth dip). Replaces extract_emf (inject_extract.c:123-213); the caller
+ * stores complex64 where the reference does (emf.h:42). */
+int csem_extract_host(csem_ctx *c, int nch, const int *ch, int nrec, const float *rec, const double *x,
+                      double *out);
+
+/* ------------------------------------------------------------ FP64 solve of one system
+ * The dispatch of main.c:104-118 on a device-resident system: algopt 1 = BiCGStab,
+ * 2 = GMRES(nrestart); preco 0 none, 1 LU-SGS, 2 inner GMRES(mp), 3 A-phi. niter is
+ * the reference's iteration limit (GMRES runs niter/nrestart restart cycles, as
+ * main.c:106,109). Replaces bicgstab/fbicgstab/gmres/fgmres (solver.c:16-512).
+ * x: initial guess in, solution out. hist receives the relative residuals in order
+ * (*nhist of them, at most hist_cap copied); *iters the iterations (BiCGStab) or cycles
+ * (GMRES); *status a CSEM_ST_* value. */
+#define CSEM_ST_RUNNING 0
+#define CSEM_ST_CONVERGED 1
+#define CSEM_ST_MAXITER 2
+#define CSEM_ST_BREAKDOWN 3
+#define CSEM_ST_NONFINITE 4
+#define CSEM_ST_ZERO_RHS 5
+int csem_solve_fp64_host(csem_ctx *c, int algopt, int preco, int niter, double tol, int nrestart, int mp,
+                         double iom_re, double iom_im, const double *b, double *x, double *hist, int hist_cap,
+                         int *nhist, int *iters, int *status);
+
+/* ------------------------------------------------------------ device-pointer entry points
+ * For callers that keep vectors in GPU memory. nsys systems are stored back to back
+ * (stride lE); iom is a host array of nsys (re, im) pairs. prec: 64 = complex128,
+ * 32 = complex64. */
+int csem_fdfd_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
+int csem_lusgs_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
+int csem_aphi_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
+/* out[s] (complex128, device) = <a_s, b_s> for nsys vectors of length n (stride n) */
+int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
+/* synchronise the context's stream */
+int csem_ctx_sync(csem_ctx *c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,97 @@
+"""The C ABI library loads without a GPU and exports every function its headers declare."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(\w+)\s*\([^;{]*\)\s*;", src, flags=re.M):
+            if not m.group(0).lstrip().startswith(("typedef", "#")):
+                names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = declared_functions()
+    assert "csem_fdfd_apply_host" in names and "csem_grid_extend" in names and len(names) > 30
+
+
+def test_library_exports_every_declared_symbol(csem_lib):
+    lib = ctypes.CDLL(csem_lib._name)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_no_device_is_reported_not_faked(csem_lib):
+    import demo_matrixfree_csem_gb300 as cs
+    if cs.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    from cases import GOLDEN_CASES, load_golden, parse_args, product_grid
+    d, args, gold = load_golden(GOLDEN_CASES[0])
+    G = product_grid(d, parse_args(args))
+    with pytest.raises(cs.CsemError) as e:
+        cs.Ctx(G, 0, 0)
+    assert e.value.code == -6
+    with pytest.raises(cs.CsemError):
+        cs.cdot(np.ones(4), np.ones(4))
+
+
+def test_getpar_semantics(csem_lib, tmp_path):
+    import demo_matrixfree_csem_gb300 as cs
+    L = cs.lib()
+    pf = tmp_path / "par.txt"
+    pf.write_text("nb=7 freqs=1,2 'name=a b'\n tol=1e-3\n")
+    argv = [b"prog", b"nb=3", b"freqs=0.25,0.75,1.25", b"junk", b"nb=10", f"par={pf}".encode(), b"rho_air=1e6"]
+    arr = (ctypes.c_char_p * len(argv))(*argv)
+    L.csem_initargs(len(argv), arr)
+    v = ctypes.c_int()
+    assert L.csem_getparint(b"nb", ctypes.byref(v)) == 1 and v.value == 10   # last occurrence wins
+    assert L.csem_countparval(b"freqs") == 3                                    # command line overrides par file
+    f = (ctypes.c_float * 3)()
+    assert L.csem_getparfloat(b"freqs", f) == 3
+    assert f[0] == np.float32(0.25) and f[2] == np.float32(1.25)
+    t = ctypes.c_float()
+    assert L.csem_getparfloat(b"tol", ctypes.byref(t)) == 1 and t.value == np.float32(1e-3)  # from par file
+    assert L.csem_getparint(b"missing", ctypes.byref(v)) == 0
+
+
+def test_freq_sort_and_emf_writer(csem_lib, tmp_path):
+    import demo_matrixfree_csem_gb300 as cs
+    L = cs.lib()
+    f = np.array([1.25, 0.25, 0.75], np.float32)
+    L.csem_sort_freqs(f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 3)
+    assert list(f) == [np.float32(0.25), np.float32(0.75), np.float32(1.25)]
+    d = np.arange(2 * 3 * 2, dtype=np.complex64).reshape(2, 3, 2) * (1.5 - 0.5j)
+    fn = str(tmp_path / "emf_0001.txt")
+    assert L.csem_write_emf(fn.encode(), 1, 2, 3, 2, d.view(np.float32).ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+    lines = open(fn).read().splitlines()
+    assert lines[0] == "iTx \t iRx    ichrec  ifreq \t emf_real \t emf_imag"
+    assert lines[1] == "1 \t 1 \t 1 \t 1 \t %e \t %e" % (d[0, 0, 0].real, d[0, 0, 0].imag)
+    assert lines[4] == "1 \t 2 \t 1 \t 2 \t %e \t %e" % (d[0, 1, 1].real, d[0, 1, 1].imag)
+    assert len(lines) == 1 + 12
+
+
+def test_input_errors_are_codes(csem_lib, tmp_path):
+    import demo_matrixfree_csem_gb300 as cs
+    with pytest.raises(cs.CsemError) as e:
+        cs.Grid.from_files(*(str(tmp_path / n) for n in ("fx1", "fx2", "fx3", "r1", "r2", "r3")))
+    assert e.value.code == -2
+    (tmp_path / "fx1").write_bytes(np.arange(4, dtype=np.float32).tobytes())
+    (tmp_path / "fx2").write_bytes(np.arange(4, dtype=np.float32).tobytes())
+    (tmp_path / "fx3").write_bytes(np.arange(4, dtype=np.float32).tobytes())
+    for n in ("r1", "r2", "r3"):
+        (tmp_path / n).write_bytes(np.ones(20, np.float32).tobytes())  # 27 needed: short file
+    with pytest.raises(cs.CsemError) as e:
+        cs.Grid.from_files(*(str(tmp_path / n) for n in ("fx1", "fx2", "fx3", "r1", "r2", "r3")))
+    assert e.value.code == -2 and "size not match" in str(e.value)

@@ -1,0 +1,163 @@
+"""GPU kernels against the oracle and the reference's golden fixtures, through the C ABI.
+
+Tolerances:
+  * complex128 operators, preconditioners, injection, extraction: bit-identical to the
+    reference (no FFT involved) - asserted with array_equal;
+  * anything through the airwave FFT (cuFFT vs the oracle's radix-2 DFT): max-norm
+    relative difference <= 1e-12;
+  * dot products (parallel tree vs sequential sum): <= 1e-13 relative;
+  * complex64 operators vs the complex128 oracle: <= 2e-5 relative (max norm);
+  * short FP64 solves (different dot summation order only): <= 1e-9 relative.
+"""
+import numpy as np
+import pytest
+
+import demo_matrixfree_csem_gb300 as cs
+from cases import (GOLDEN_CASES, channels, load_golden, oracle_for, parse_args, probe, product_grid, read_rows,
+                   relerr, tol_of)
+from demo_matrixfree_csem_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(case):
+    d, args, gold = load_golden(case)
+    p = parse_args(args)
+    G = product_grid(d, p)
+    return d, p, gold, G, cs.Ctx(G, int(p.get("airbc", 0)), int(p.get("fvm", 0)))
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_fdfd_apply_fp64(gpu, case):
+    d, p, gold, G, ctx = _ctx(case)
+    y = ctx.fdfd_apply(cs.iom_of(gold["freqs"][0]), gold["x"])
+    if int(p.get("airbc", 0)):
+        assert relerr(y, gold["Ax"]) <= 1e-12
+    else:
+        assert np.array_equal(y, gold["Ax"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_preconditioner_fp64_bit_exact(gpu, case):
+    d, p, gold, G, ctx = _ctx(case)
+    preco = int(p.get("preco", 1))
+    if preco not in (1, 3):
+        pytest.skip("no LU-SGS / A-phi in this case")
+    iom = cs.iom_of(gold["freqs"][0])
+    y = ctx.lusgs_apply(iom, gold["x"]) if preco == 1 else ctx.aphi_apply(iom, gold["x"])
+    assert np.array_equal(y, gold["Mx"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_inject_extract_bit_exact(gpu, case):
+    d, p, gold, G, ctx = _ctx(case)
+    iom = cs.iom_of(gold["freqs"][0])
+    src = read_rows(f"{d}/sources.txt")[0]
+    b = ctx.inject_source(iom, channels(p, "chsrc"), src)
+    assert np.array_equal(b, gold["b"])
+    rec = read_rows(f"{d}/receivers.txt")
+    out = ctx.extract_emf(channels(p, "chrec"), rec, gold["x_solve"])
+    assert np.array_equal(out.astype(np.complex64), gold["dcal"])
+    O = oracle_for(G, p)
+    assert np.array_equal(out, O.extract(channels(p, "chrec"), rec, gold["x_solve"]))
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_short_solve_tracks_reference(gpu, case):
+    d, p, gold, G, ctx = _ctx(case)
+    iom = cs.iom_of(gold["freqs"][0])
+    b = gold["b"]
+    x, hist, it, st = ctx.solve_fp64(iom, b, algopt=int(p["algopt"]), preco=int(p["preco"]), niter=int(p["niter"]),
+                                     tol=tol_of(p, 0, gold["freqs"]), nrestart=int(p.get("nrestart", 10)),
+                                     mp=int(p.get("mp", 30)))
+    assert relerr(x, gold["x_solve"]) <= 1e-9
+    printed = gold["hist_printed"]
+    np.testing.assert_allclose(hist[:len(printed)], printed, rtol=2e-6)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_c64_operators_close_to_fp64(gpu, case):
+    d, p, gold, G, ctx = _ctx(case)
+    iom = cs.iom_of(gold["freqs"][0])
+    x = gold["x"]
+    assert relerr(ctx.fdfd_apply(iom, x, c64=True), gold["Ax"]) <= 2e-5
+    preco = int(p.get("preco", 1))
+    if preco == 1:
+        assert relerr(ctx.lusgs_apply(iom, x, c64=True), gold["Mx"]) <= 2e-5
+    elif preco == 3:
+        assert relerr(ctx.aphi_apply(iom, x, c64=True), gold["Mx"]) <= 2e-5
+
+
+@pytest.mark.parametrize("airbc,fvm", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_larger_grid_bit_exact(gpu, tmp_path, airbc, fvm):
+    """A grid spanning several CTAs in every direction and several k-chunks."""
+    cfg = synthetic.random_small(21 + airbc + 2 * fvm, nx=40, ny=27, nz=19, nb=4, airbc=airbc, fvm=fvm,
+                                 n1fft=64, n2fft=64)
+    synthetic.write_config(cfg, str(tmp_path))
+    p = dict(cfg.params, nb=4)
+    G = product_grid(str(tmp_path), {k: str(v) for k, v in p.items()})
+    ctx = cs.Ctx(G, airbc, fvm)
+    O = oracle_for(G, {k: str(v) for k, v in p.items()})
+    f = 0.75
+    O.set_freq(f)
+    iom = cs.iom_of(f)
+    x = probe(ctx.lE, 5)
+    ya = ctx.fdfd_apply(iom, x)
+    yo = O.fdfd(x)
+    if airbc:
+        assert relerr(ya, yo) <= 1e-12
+    else:
+        assert np.array_equal(ya, yo)
+    assert np.array_equal(ctx.lusgs_apply(iom, x), O.lusgs(x))
+
+
+@pytest.mark.parametrize("airbc", [0, 1])
+def test_aphi_larger_grid_bit_exact(gpu, tmp_path, airbc):
+    cfg = synthetic.random_small(31 + airbc, nx=33, ny=21, nz=17, nb=3, airbc=airbc, n1fft=32, n2fft=32, preco=3)
+    synthetic.write_config(cfg, str(tmp_path))
+    p = {k: str(v) for k, v in cfg.params.items()}
+    G = product_grid(str(tmp_path), p)
+    ctx = cs.Ctx(G, airbc, 0)
+    O = oracle_for(G, p)
+    O.set_freq(1.0)
+    x = probe(ctx.lE, 6)
+    assert np.array_equal(ctx.aphi_apply(cs.iom_of(1.0), x), O.aphi(x))
+
+
+def test_airwave_ghosts(gpu, tmp_path):
+    cfg = synthetic.random_small(41, nx=30, ny=26, nz=10, nb=4, airbc=1, n1fft=128, n2fft=128)
+    synthetic.write_config(cfg, str(tmp_path))
+    p = {k: str(v) for k, v in cfg.params.items()}
+    G = product_grid(str(tmp_path), p)
+    ctx = cs.Ctx(G, 1, 0)
+    O = oracle_for(G, p)
+    hz0 = probe(ctx.n1 * ctx.n2, 7)
+    hx, hy = ctx.airbc_apply(hz0)
+    ox, oy = O.airbc(hz0)
+    assert relerr(hx, ox) <= 1e-12 and relerr(hy, oy) <= 1e-12
+
+
+def test_dot_products(gpu):
+    from oracle import Oracle
+    rng = np.random.default_rng(3)
+    for n in (1, 31, 1000, 300001):
+        a = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        ref = Oracle.cdot(a, b)
+        got = cs.cdot(a, b)
+        assert abs(got - ref) <= 1e-13 * np.sqrt(n) * np.abs(a).max() * np.abs(b).max() * 4
+        a32, b32 = a.astype(np.complex64), b.astype(np.complex64)
+        exact = np.sum(a32.astype(np.complex128) * np.conj(b32.astype(np.complex128)))
+        got32 = cs.cdot(a32, b32, c64=True)
+        assert abs(got32 - exact) <= 1e-12 * np.sum(np.abs(a32) * np.abs(b32)) + 1e-300
+    # deterministic: the same call twice gives the same bits
+    a = rng.standard_normal(50000) + 1j * rng.standard_normal(50000)
+    assert cs.cdot(a, a[::-1].copy()) == cs.cdot(a, a[::-1].copy())
+
+
+def test_gmres_preconditioner(gpu):
+    d, p, gold, G, ctx = _ctx("gmrespre_air0")
+    O = oracle_for(G, p)
+    O.set_freq(float(gold["freqs"][0]))
+    y = ctx.gmres_apply(cs.iom_of(gold["freqs"][0]), gold["x"], mp=5)
+    assert relerr(y, O.gmres_pre(gold["x"], 5)) <= 1e-10

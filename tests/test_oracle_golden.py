@@ -1,0 +1,61 @@
+"""The CPU oracle and the product's host set-up, pinned against fixtures produced by the
+reference itself (tests/golden, generated by tests/golden/make_golden.py from the
+reference built from its sources). Runs anywhere, no GPU."""
+import numpy as np
+import pytest
+
+from cases import GOLDEN_CASES, channels, load_golden, oracle_for, parse_args, product_grid, read_rows, tol_of
+
+GRID_KEYS = ("x1", "x2", "x3", "x1s", "x2s", "x3s", "d1", "d2", "d3", "d1s", "d2s", "d3s",
+             "sigma11", "sigma22", "sigma33")
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_host_setup_matches_reference(case):
+    d, args, gold = load_golden(case)
+    p = parse_args(args)
+    G = product_grid(d, p)
+    A = G.arrays()
+    for k in GRID_KEYS:
+        assert np.array_equal(A[k], gold[k]), k
+    if "sH1" in gold:
+        assert np.array_equal(A["sH1"], gold["sH1"])
+        assert np.array_equal(A["sH2"], gold["sH2"])
+    assert np.float32(G.g.rho_water) == np.float32(gold["rho_water"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_oracle_operators_bit_exact(case):
+    d, args, gold = load_golden(case)
+    p = parse_args(args)
+    O = oracle_for(product_grid(d, p), p)
+    O.set_freq(float(gold["freqs"][0]))
+    x = gold["x"]
+    assert np.array_equal(O.fdfd(x), gold["Ax"])
+    preco = int(p.get("preco", 1))
+    if preco == 1:
+        assert np.array_equal(O.lusgs(x), gold["Mx"])
+    elif preco == 3:
+        assert np.array_equal(O.aphi(x), gold["Mx"])
+    src = read_rows(f"{d}/sources.txt")[0]
+    assert np.array_equal(O.inject(channels(p, "chsrc"), src), gold["b"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_oracle_solver_bit_exact(case):
+    d, args, gold = load_golden(case)
+    p = parse_args(args)
+    O = oracle_for(product_grid(d, p), p)
+    O.set_freq(float(gold["freqs"][0]))
+    src = read_rows(f"{d}/sources.txt")[0]
+    b = O.inject(channels(p, "chsrc"), src)
+    x, hist, it = O.solve(b, algopt=int(p["algopt"]), precond=int(p["preco"]), niter=int(p["niter"]),
+                          tol=tol_of(p, 0, gold["freqs"]), nrestart=int(p.get("nrestart", 10)),
+                          mp=int(p.get("mp", 30)))
+    assert np.array_equal(x, gold["x_solve"])
+    printed = gold["hist_printed"]
+    # the reference prints %e (7 significant digits) and not the final value
+    np.testing.assert_allclose(hist[:len(printed)], printed, rtol=6e-7, atol=0)
+    rec = read_rows(f"{d}/receivers.txt")
+    out = O.extract(channels(p, "chrec"), rec, x)
+    assert np.array_equal(out.astype(np.complex64), gold["dcal"])
