@@ -103,6 +103,10 @@ def lib(build_if_missing: bool = True):
         "csem_lusgs_apply_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p]),
         "csem_aphi_apply_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p]),
         "csem_cdot_dev": (C.c_int, [C.c_int, C.c_long, C.c_int, C.c_void_p, C.c_void_p, _dp, C.c_void_p]),
+        "csem_solve_batch_host": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, C.c_int, _ip, C.c_int, _ip, C.c_int, _fp,
+                                            C.c_void_p, _dp, _ip, _ip, _ip, _dp]),
+        "csem_profile": (C.c_int, [C.c_int]),
+        "csem_profile_read": (C.c_int, [C.c_int, _dp, _lp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -301,6 +305,53 @@ class Ctx:
                                           _p(b.view(np.float64)), _p(x.view(np.float64)), _p(hist), cap,
                                           C.byref(nh), C.byref(it), C.byref(st)))
         return x, hist[:min(nh.value, cap)].copy(), it.value, STATUS.get(st.value, st.value)
+
+
+class _BatchOpts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("algopt", C.c_int), ("preco", C.c_int), ("niter", C.c_int),
+                ("tol", C.c_float), ("inner_tol", C.c_double), ("check_every", C.c_int), ("max_outer", C.c_int),
+                ("nrestart", C.c_int), ("mp", C.c_int)]
+
+
+def solve_batch(ctx: Ctx, freqs, srcs, chsrc=("Ex",), chrec=("Ex", "Ey", "Ez"), rec=None, precision=32, algopt=1,
+                preco=1, niter=1000, tol=1e-8, inner_tol=1e-4, check_every=4, max_outer=30, nrestart=10, mp=30):
+    """Solve len(freqs) systems (frequency freqs[s], dipole at srcs[s]) and extract the
+    receivers rec ([nrec][5] rows). Returns a dict with dcal [nsys][nchrec][nrec]
+    (complex128), iters, outer, status, relres."""
+    f = np.ascontiguousarray(freqs, np.float32)
+    s = np.ascontiguousarray(np.asarray(srcs, np.float32)[:, :3])
+    nsys = len(f)
+    assert s.shape == (nsys, 3)
+    cs_ = np.asarray([CHANNELS[c] if isinstance(c, str) else c for c in chsrc], np.int32)
+    cr = np.asarray([CHANNELS[c] if isinstance(c, str) else c for c in chrec], np.int32)
+    r = np.ascontiguousarray(rec if rec is not None else np.zeros((0, 5)), np.float32)
+    o = _BatchOpts(precision, algopt, preco, niter, tol, inner_tol, check_every, max_outer, nrestart, mp)
+    dcal = np.zeros((nsys, len(cr), len(r)), np.complex128)
+    it = np.zeros(nsys, np.int32)
+    ou = np.zeros(nsys, np.int32)
+    st = np.zeros(nsys, np.int32)
+    rr = np.zeros(nsys)
+    _check(lib().csem_solve_batch_host(ctx.h, nsys, _p(f, _fp), _p(s, _fp), len(cs_), _p(cs_, _ip), len(cr),
+                                       _p(cr, _ip), len(r), _p(r, _fp), C.byref(o), _p(dcal.view(np.float64)),
+                                       _p(it, _ip), _p(ou, _ip), _p(st, _ip), _p(rr)))
+    return dict(dcal=dcal, iters=it, outer=ou, status=[STATUS.get(int(v), int(v)) for v in st], relres=rr)
+
+
+PROF_NAMES = ["A64", "A32", "lusgs64", "lusgs32", "aphi64", "aphi32", "air64", "air32", "stencil64", "stencil32"]
+
+
+def profile(enable: bool) -> None:
+    """Start (clearing earlier records) or stop per-operator device timing."""
+    _check(lib().csem_profile(1 if enable else 0))
+
+
+def profile_read() -> dict:
+    """{category: (milliseconds, applications)} from the recorded CUDA events."""
+    n = len(PROF_NAMES)
+    ms = np.zeros(n)
+    cnt = np.zeros(n, np.int64)
+    _check(lib().csem_profile_read(n, _p(ms), cnt.ctypes.data_as(_lp)))
+    return {PROF_NAMES[i]: (float(ms[i]), int(cnt[i])) for i in range(n)}
 
 
 def cdot(a, b, c64=False) -> complex:

@@ -7,6 +7,7 @@
 #include "../../include/csem_gpu.h"
 #include "engine_model.h"
 #include "solve_fp64.h"
+#include "solve_mixed.h"
 
 extern "C" int csem_set_error(int code, const char* fmt, ...);
 
@@ -18,6 +19,7 @@ struct csem_ctx {
   Ops<F64>* ops64 = nullptr;
   Ops<F32>* ops32 = nullptr;
   Solver64* solver = nullptr;
+  MixedBatch* batch = nullptr;
   DevBuf io[4], sc64, sc32, dotp;
   int nmax64 = 0, nmax32 = 0;
 };
@@ -108,6 +110,7 @@ void csem_ctx_destroy(csem_ctx* c)
 {
   if (!c) return;
   cudaStreamSynchronize(c->st);
+  delete c->batch;
   delete c->solver;
   delete c->ops64;
   delete c->ops32;
@@ -347,6 +350,106 @@ int csem_solve_fp64_host(csem_ctx* c, int algopt, int preco, int niter, double t
   if (nhist) *nhist = (int)h.size();
   if (iters) *iters = it;
   if (status) *status = st;
+  API_END
+}
+
+// ---------------------------------------------------------------- many systems
+static MixedBatch* batch_for(csem_ctx* c, int nsys)
+{
+  if (!c->batch || c->batch->nsys != nsys) {
+    delete c->batch;
+    c->batch = nullptr;
+    c->batch = new MixedBatch(c->model, nsys, c->st);
+  }
+  return c->batch;
+}
+
+int csem_solve_batch_host(csem_ctx* c, int nsys, const float* freq, const float* src3, int nchsrc, const int* chsrc,
+                          int nchrec, const int* chrec, int nrec, const float* rec, const csem_batch_opts* opt,
+                          double* dcal, int* iters, int* outer, int* status, double* relres)
+{
+  if (nsys < 1) return csem_set_error(CSEM_EINVAL, "nsys must be >= 1");
+  if (!opt || (opt->precision != 32 && opt->precision != 64))
+    return csem_set_error(CSEM_EINVAL, "precision must be 32 or 64");
+  if (opt->precision == 32 && !(opt->preco == 1 || opt->preco == 3))
+    return csem_set_error(CSEM_EINVAL, "the mixed-precision solver takes preco 1 (LU-SGS) or 3 (A-phi)");
+  if (opt->precision == 32 && opt->algopt != 1)
+    return csem_set_error(CSEM_EINVAL, "the mixed-precision solver runs BiCGStab (algopt=1)");
+  if (nchsrc < 1 || nchsrc > 8) return csem_set_error(CSEM_EINVAL, "1..8 source channels");
+  API_BEGIN
+  std::vector<double> iom(2 * nsys), tol(nsys);
+  for (int s = 0; s < nsys; s++) {
+    const double pi = 3.14159265358979323846264, mu0 = 4. * pi * 1e-7;
+    iom[2 * s] = 0.0;
+    iom[2 * s + 1] = ((2. * pi) * (double)freq[s]) * mu0;  // main.c:95
+    const float tf = opt->tol / freq[s];                        // main.c:94, in float
+    tol[s] = (double)tf;
+  }
+  if (opt->precision == 32) {
+    MixedBatch* B = batch_for(c, nsys);
+    B->inject(src3, iom.data(), nchsrc, chsrc);
+    MixedOptions mo;
+    mo.niter = opt->niter > 0 ? opt->niter : 1000;
+    mo.max_inner_total = 3 * mo.niter;
+    mo.max_outer = opt->max_outer > 0 ? opt->max_outer : 30;
+    mo.preco = opt->preco;
+    mo.inner_tol = opt->inner_tol > 0 ? opt->inner_tol : 1e-4;
+    mo.check_every = opt->check_every > 0 ? opt->check_every : 4;
+    std::vector<MixedResult> res;
+    B->solve(iom.data(), tol.data(), mo, res);
+    B->extract(nchrec, chrec, nrec, rec, dcal);
+    for (int s = 0; s < nsys; s++) {
+      if (iters) iters[s] = res[s].inner_iters;
+      if (outer) outer[s] = res[s].outer;
+      if (status) status[s] = res[s].status;
+      if (relres) relres[s] = res[s].relres;
+    }
+  } else {
+    Solver64* S = solver_for(c);
+    Model* m = c->model;
+    const size_t bytes = sizeof(double2) * (size_t)m->lE;
+    ensure(c->io[0], bytes);
+    ensure(c->io[1], bytes);
+    ensure(c->io[2], 256);
+    ensure(c->io[3], sizeof(double2) * (size_t)nchrec * (nrec > 0 ? nrec : 1) + sizeof(float) * 5 * (size_t)nrec +
+                         sizeof(int) * (nchrec + nchsrc) + 64);
+    for (int s = 0; s < nsys; s++) {
+      S->set_iom(iom[2 * s], iom[2 * s + 1]);
+      double2 io = make_double2(iom[2 * s], iom[2 * s + 1]);
+      char stage[64 + 8 * sizeof(int)];
+      memcpy(stage, src3 + 3 * s, sizeof(float) * 3);
+      memcpy(stage + 16, &io, sizeof(io));
+      memcpy(stage + 64, chsrc, sizeof(int) * nchsrc);
+      CSEM_CUDA_TRY(cudaMemcpyAsync(c->io[2].p, stage, sizeof(stage), cudaMemcpyHostToDevice, c->st));
+      CSEM_CUDA_TRY(cudaMemsetAsync(c->io[0].p, 0, bytes, c->st));
+      char* d2 = c->io[2].as<char>();
+      launch_inject(m->acq, 1, (const float*)d2, (const double2*)(d2 + 16), (const int*)(d2 + 64), nchsrc,
+                    c->io[0].as<double2>(), c->st);
+      CSEM_CUDA_TRY(cudaMemsetAsync(c->io[1].p, 0, bytes, c->st));
+      std::vector<double> h;
+      int st = ST_RUNNING, it;
+      const int niter = opt->niter > 0 ? opt->niter : 1000;
+      if (opt->algopt == 2)
+        it = S->gmres(opt->preco, opt->mp, c->io[1].as<double2>(), c->io[0].as<double2>(), niter / opt->nrestart,
+                      tol[s], opt->nrestart, h, st);
+      else
+        it = S->fbicgstab(opt->preco, opt->mp, c->io[1].as<double2>(), c->io[0].as<double2>(), niter, tol[s], h, st,
+                          opt->preco != 0);
+      char* d3 = c->io[3].as<char>();
+      const size_t ob = sizeof(double2) * (size_t)nchrec * nrec, rb = sizeof(float) * 5 * (size_t)nrec;
+      CSEM_CUDA_TRY(cudaMemcpyAsync(d3 + ob, rec, rb, cudaMemcpyHostToDevice, c->st));
+      CSEM_CUDA_TRY(cudaMemcpyAsync(d3 + ob + rb, chrec, sizeof(int) * nchrec, cudaMemcpyHostToDevice, c->st));
+      launch_extract<double2>(m->acq, 1, nchrec, (const int*)(d3 + ob + rb), nrec, (const float*)(d3 + ob),
+                              c->io[1].as<double2>(), m->lE, nullptr, (double2*)d3, c->st);
+      CSEM_CUDA_TRY(cudaGetLastError());
+      CSEM_CUDA_TRY(cudaMemcpyAsync(dcal + 2 * (size_t)s * nchrec * nrec, d3, ob, cudaMemcpyDeviceToHost, c->st));
+      CSEM_CUDA_TRY(cudaStreamSynchronize(c->st));
+      if (iters) iters[s] = it;
+      if (outer) outer[s] = 0;
+      if (status) status[s] = st;
+      if (relres) relres[s] = h.empty() ? 0.0 : h.back();
+    }
+  }
   API_END
 }
 

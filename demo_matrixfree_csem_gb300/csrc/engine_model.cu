@@ -5,6 +5,7 @@
 #include <utility>
 #include <vector>
 #include "engine_model.h"
+#include "prof.h"
 #include "../../include/csem_host.h"
 
 namespace csem {
@@ -309,17 +310,23 @@ void Ops<P>::zero(C* Y, long n, int nslot, const int* sys_list)
 template <class P>
 void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
 {
+  ProfScope whole(P::exact ? PROF_A64 : PROF_A32, st);
   const GridP<P>& g = m->grid<P>();
   if (m->airbc) {
     const AirP<P>& a = m->air<P>();
-    launch_hz0<P>(g, sc, X, hz0.as<C>(), nslot, sys_list, st);
-    launch_air_gather<P>(a, hz0.as<C>(), K.as<C>(), nslot, st);
-    fft->exec(P::exact, K.p, nslot, CUFFT_FORWARD, st);
-    launch_air_filter<P>(a, K.as<C>(), K2.as<C>(), nslot, st);
-    fft->exec(P::exact, K2.p, 2 * nslot, CUFFT_INVERSE, st);
-    launch_air_scatter<P>(a, K2.as<C>(), ghx.as<C>(), ghy.as<C>(), nslot, st);
+    {
+      ProfScope air(P::exact ? PROF_AIR64 : PROF_AIR32, st);
+      launch_hz0<P>(g, sc, X, hz0.as<C>(), nslot, sys_list, st);
+      launch_air_gather<P>(a, hz0.as<C>(), K.as<C>(), nslot, st);
+      fft->exec(P::exact, K.p, nslot, CUFFT_FORWARD, st);
+      launch_air_filter<P>(a, K.as<C>(), K2.as<C>(), nslot, st);
+      fft->exec(P::exact, K2.p, 2 * nslot, CUFFT_INVERSE, st);
+      launch_air_scatter<P>(a, K2.as<C>(), ghx.as<C>(), ghy.as<C>(), nslot, st);
+    }
+    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st);
     launch_fdfd<P>(g, sc, X, Y, ghx.as<C>(), ghy.as<C>(), nslot, sys_list, st);
   } else {
+    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st);
     launch_fdfd<P>(g, sc, X, Y, nullptr, nullptr, nslot, sys_list, st);
   }
 }
@@ -327,6 +334,7 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
 template <class P>
 void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
 {
+  ProfScope prof(P::exact ? PROF_LUSGS64 : PROF_LUSGS32, st);
   SweepP<P> s;
   memset(&s, 0, sizeof(s));
   s.g = m->grid<P>();
@@ -358,6 +366,7 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
 template <class P>
 void Ops<P>::apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
 {
+  ProfScope prof(P::exact ? PROF_APHI64 : PROF_APHI32, st);
   if (!V.p) {
     V.alloc(sizeof(C) * (size_t)m->lv * nmax);
     BV.alloc(sizeof(C) * (size_t)m->lv * nmax);

@@ -178,6 +178,7 @@ __global__ void k_vec_s(long n, const int* __restrict__ sys_list, const KrylovSc
                         typename P::C* __restrict__ s)
 {
   CSEM_VEC_PROLOGUE
+  if (ks[sys].status != ST_RUNNING) return;  // finished systems keep their vectors
   const typename P::C alpha = cast_c<P>(ks[sys].alpha);
   s[o] = csub<P>(r[o], cmul<P>(alpha, v[o]));
 }
@@ -191,6 +192,7 @@ __global__ void k_vec_xr(long n, const int* __restrict__ sys_list, const KrylovS
                          const typename P::C* __restrict__ t)
 {
   CSEM_VEC_PROLOGUE
+  if (ks[sys].status != ST_RUNNING) return;
   const typename P::C alpha = cast_c<P>(ks[sys].alpha), omega = cast_c<P>(ks[sys].omega);
   const typename P::C ss = SS_IS_S ? s[o] : r[o];
   x[o] = cadd<P>(x[o], cadd<P>(cmul<P>(alpha, pp[o]), cmul<P>(omega, ss)));
@@ -204,6 +206,7 @@ __global__ void k_vec_p(long n, const int* __restrict__ sys_list, const KrylovSc
                         const typename P::C* __restrict__ v)
 {
   CSEM_VEC_PROLOGUE
+  if (ks[sys].status != ST_RUNNING) return;
   const typename P::C beta = cast_c<P>(ks[sys].beta), omega = cast_c<P>(ks[sys].omega);
   p[o] = cadd<P>(r[o], cmul<P>(beta, csub<P>(p[o], cmul<P>(omega, v[o]))));
 }

@@ -1,0 +1,90 @@
+// Per-operator device timing (see prof.h) and its C entry points.
+#include <vector>
+#include "../../include/csem_gpu.h"
+#include "prof.h"
+
+namespace csem {
+
+namespace {
+struct Rec {
+  int cat;
+  cudaEvent_t a, b;
+  bool closed;
+};
+bool g_on = false;
+std::vector<Rec> g_recs;
+std::vector<cudaEvent_t> g_pool;
+
+cudaEvent_t get_event()
+{
+  if (!g_pool.empty()) {
+    cudaEvent_t e = g_pool.back();
+    g_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+}  // namespace
+
+bool prof_on() { return g_on; }
+
+int prof_begin(int cat, cudaStream_t st)
+{
+  Rec r;
+  r.cat = cat;
+  r.a = get_event();
+  r.b = get_event();
+  r.closed = false;
+  cudaEventRecord(r.a, st);
+  g_recs.push_back(r);
+  return (int)g_recs.size() - 1;
+}
+
+void prof_end(int tok, cudaStream_t st)
+{
+  if (tok < 0 || tok >= (int)g_recs.size()) return;
+  cudaEventRecord(g_recs[tok].b, st);
+  g_recs[tok].closed = true;
+}
+
+}  // namespace csem
+
+extern "C" {
+
+/* Enable (1) or disable (0) per-operator timing; enabling clears earlier records. */
+int csem_profile(int enable)
+{
+  using namespace csem;
+  cudaDeviceSynchronize();
+  for (auto& r : g_recs) {
+    g_pool.push_back(r.a);
+    g_pool.push_back(r.b);
+  }
+  g_recs.clear();
+  g_on = enable != 0;
+  return CSEM_OK;
+}
+
+/* ms[cat] = summed device milliseconds, count[cat] = applications, cat < ncat. */
+int csem_profile_read(int ncat, double* ms, long* count)
+{
+  using namespace csem;
+  cudaDeviceSynchronize();
+  for (int c = 0; c < ncat; c++) {
+    ms[c] = 0;
+    count[c] = 0;
+  }
+  for (auto& r : g_recs) {
+    if (!r.closed || r.cat >= ncat) continue;
+    float t = 0;
+    if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+      ms[r.cat] += t;
+      count[r.cat] += 1;
+    }
+  }
+  return CSEM_OK;
+}
+
+}  // extern "C"

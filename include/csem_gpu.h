@@ -95,6 +95,37 @@ int csem_solve_fp64_host(csem_ctx *c, int algopt, int preco, int niter, double t
                          double iom_re, double iom_im, const double *b, double *x, double *hist, int hist_cap,
                          int *nhist, int *iters, int *status);
 
+/* ------------------------------------------------------------ many systems at once
+ * Solve nsys independent systems (frequency freq[s], unit dipole at src3[s] on the
+ * channels chsrc) on the context's model and extract the receivers. This replaces the
+ * reference driver's per-frequency loop (main.c:93-123: injection, timed solve,
+ * extraction) for every (frequency, source) pair at once; the reference itself solves
+ * only the first source row (acq_init_free.c:56,90).
+ *   precision 32: batched mixed precision - complex64 flexible BiCGStab with complex64
+ *                 LU-SGS (preco 1) or A-phi (preco 3) inside complex128 defect
+ *                 correction; a system stops when |b - A x| / |b| < tol/f (complex128,
+ *                 true residual);
+ *   precision 64: the plain complex128 solver of csem_solve_fp64_host, one system after
+ *                 the other (algopt/preco/nrestart/mp as the reference).
+ * Outputs per system: dcal [nsys][nchrec][nrec] complex128 receivers, iters (inner
+ * complex64 iterations, or complex128 iterations / GMRES cycles), outer (defect-
+ * correction cycles), status (CSEM_ST_*), relres (final relative residual). */
+typedef struct csem_batch_opts {
+  int precision;     /* 32 or 64 */
+  int algopt;        /* 1 BiCGStab, 2 GMRES (precision 64 only) */
+  int preco;         /* 0 none, 1 LU-SGS, 2 inner GMRES (64 only), 3 A-phi */
+  int niter;         /* the reference's niter */
+  float tol;         /* the reference's tol; system s stops at tol/freq[s] in float (main.c:94) */
+  double inner_tol;  /* precision 32: relative reduction of one inner solve (<= 0: 1e-4) */
+  int check_every;   /* precision 32: inner iterations between status reads (<= 0: 4) */
+  int max_outer;     /* precision 32: defect-correction cycles (<= 0: 30) */
+  int nrestart, mp;  /* precision 64: GMRES(nrestart) and GMRES(mp) preconditioner */
+} csem_batch_opts;
+int csem_solve_batch_host(csem_ctx *c, int nsys, const float *freq, const float *src3, int nchsrc,
+                          const int *chsrc, int nchrec, const int *chrec, int nrec, const float *rec,
+                          const csem_batch_opts *opt, double *dcal, int *iters, int *outer, int *status,
+                          double *relres);
+
 /* ------------------------------------------------------------ device-pointer entry points
  * For callers that keep vectors in GPU memory. nsys systems are stored back to back
  * (stride lE); iom is a host array of nsys (re, im) pairs. prec: 64 = complex128,
@@ -106,6 +137,15 @@ int csem_aphi_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, cons
 int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
 /* synchronise the context's stream */
 int csem_ctx_sync(csem_ctx *c);
+
+/* ------------------------------------------------------------ timing
+ * Per-operator device time from CUDA events recorded on the operator's stream around
+ * every application (no counterpart in the reference, which times only whole solves,
+ * main.c:103,119). Categories: 0/1 A (complex128/complex64, airwave included),
+ * 2/3 LU-SGS, 4/5 A-phi, 6/7 airwave only, 8/9 stencil kernel only.
+ * csem_profile(1) clears and starts recording, csem_profile(0) stops. */
+int csem_profile(int enable);
+int csem_profile_read(int ncat, double *ms, long *count);
 
 #ifdef __cplusplus
 }

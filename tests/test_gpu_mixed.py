@@ -1,0 +1,97 @@
+"""Batched mixed-precision solver vs the complex128 solver and the oracle.
+
+A small airwave model with two frequencies x two sources is solved three ways:
+  * the CPU oracle (the reference's arithmetic, sequential dots), system by system;
+  * the complex128 GPU path (precision 64), system by system;
+  * the batched mixed-precision GPU path (precision 32), all four systems at once.
+Receivers are compared per frequency and channel in the max norm over receivers.
+Tolerances: complex128 GPU vs oracle <= 1e-7 after convergence to tol/f (both stop at
+the same residual level, differing by dot summation order); mixed vs complex128 GPU <=
+1e-6 at tol=1e-8 (the true-residual stopping test of the mixed path is at least as
+strict as the reference's recursive-residual test).
+"""
+import numpy as np
+import pytest
+
+import demo_matrixfree_csem_gb300 as cs
+from cases import oracle_for, product_grid, relerr
+from demo_matrixfree_csem_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small_case(tmp_path_factory):
+    d = str(tmp_path_factory.mktemp("mixed"))
+    cfg = synthetic.random_small(51, nx=24, ny=20, nz=14, nb=4, airbc=1, n1fft=64, n2fft=64, freqs=(0.5, 1.0))
+    synthetic.write_config(cfg, d)
+    p = {k: str(v) for k, v in cfg.params.items()}
+    G = product_grid(d, p)
+    ctx = cs.Ctx(G, 1, 0)
+    src = np.stack([cfg.acq.src[0], cfg.acq.src[0] + np.array([37.0, -23.0, 0, 0, 0], np.float32)])
+    return cfg, G, ctx, p, src
+
+
+def _systems(cfg, src):
+    freqs = np.array([0.5, 0.5, 1.0, 1.0], np.float32)
+    srcs = np.stack([src[0], src[1], src[0], src[1]])[:, :3]
+    return freqs, srcs
+
+
+def test_fp64_batch_matches_oracle(gpu, small_case):
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    rec = cfg.acq.rec
+    r64 = cs.solve_batch(ctx, freqs, srcs, chrec=("Ex", "Ey", "Ez"), rec=rec, precision=64, preco=1, niter=400,
+                         tol=1e-8)
+    assert all(s == "converged" for s in r64["status"])
+    O = oracle_for(G, p)
+    for s in range(len(freqs)):
+        O.set_freq(float(freqs[s]))
+        b = O.inject([0], srcs[s])
+        tol = float(np.float32(np.float32(1e-8) / freqs[s]))
+        x, h, it = O.solve(b, algopt=1, precond=1, niter=400, tol=tol)
+        ref = O.extract([0, 1, 2], rec, x)
+        for c in range(3):
+            assert relerr(r64["dcal"][s, c], ref[c]) <= 1e-7, (s, c)
+        assert abs(r64["iters"][s] - it) <= max(2, 0.05 * it)
+
+
+def test_mixed_batch_matches_fp64(gpu, small_case):
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    rec = cfg.acq.rec
+    r64 = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=64, preco=1, niter=400, tol=1e-8)
+    r32 = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=32, preco=1, niter=400, tol=1e-8, inner_tol=1e-4)
+    assert all(s == "converged" for s in r32["status"]), r32
+    for s in range(len(freqs)):
+        assert r32["relres"][s] < float(np.float32(np.float32(1e-8) / freqs[s]))
+        for c in range(3):
+            assert relerr(r32["dcal"][s, c], r64["dcal"][s, c]) <= 1e-6, (s, c, relerr(r32["dcal"][s, c], r64["dcal"][s, c]))
+
+
+def test_mixed_batch_aphi(gpu, small_case):
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    rec = cfg.acq.rec
+    r = cs.solve_batch(ctx, freqs[:2], srcs[:2], rec=rec, precision=32, preco=3, niter=2000, tol=1e-8)
+    assert all(s == "converged" for s in r["status"]), r
+    ref = cs.solve_batch(ctx, freqs[:2], srcs[:2], rec=rec, precision=64, preco=1, niter=400, tol=1e-8)
+    for s in range(2):
+        for c in range(3):
+            assert relerr(r["dcal"][s, c], ref["dcal"][s, c]) <= 1e-6
+
+
+def test_batch_is_deterministic(gpu, small_case):
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    a = cs.solve_batch(ctx, freqs, srcs, rec=cfg.acq.rec, precision=32, preco=1, niter=400, tol=1e-8)
+    b = cs.solve_batch(ctx, freqs, srcs, rec=cfg.acq.rec, precision=32, preco=1, niter=400, tol=1e-8)
+    assert np.array_equal(a["dcal"], b["dcal"]) and np.array_equal(a["iters"], b["iters"])
+
+
+def test_zero_source_is_reported(gpu, small_case):
+    cfg, G, ctx, p, src = small_case
+    # a source channel code that injects nothing gives b = 0 (solver.c:116-125)
+    r = cs.solve_batch(ctx, [0.5], src[:1, :3], chsrc=(3,), rec=cfg.acq.rec, precision=32)
+    assert r["status"] == ["zero_rhs"] and np.all(r["dcal"] == 0)
