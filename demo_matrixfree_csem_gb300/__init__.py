@@ -6,5 +6,5 @@ sm_103a CUDA kernels behind a C ABI (include/csem_gpu.h, include/csem_host.h), a
 layer in C that keeps the reference's key=value driver, float32 model files and
 emf_NNNN.txt output, and Python bindings (api.py).
 """
-from .api import (CHANNELS, STATUS, CsemError, Ctx, Grid, cdot, device_count, solve_batch,  # noqa: F401
-                  iom_of, lib)
+from .api import (CHANNELS, STATUS, CsemError, Ctx, Grid, cdot, device_count, iom_of,  # noqa: F401
+                  launch_count, lib, profile, profile_read, solve_batch)

@@ -106,7 +106,8 @@ def lib(build_if_missing: bool = True):
         "csem_solve_batch_host": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, C.c_int, _ip, C.c_int, _ip, C.c_int, _fp,
                                             C.c_void_p, _dp, _ip, _ip, _ip, _dp]),
         "csem_profile": (C.c_int, [C.c_int]),
-        "csem_profile_read": (C.c_int, [C.c_int, _dp, _lp]),
+        "csem_profile_read": (C.c_int, [C.c_int, _dp, _lp, _lp]),
+        "csem_launch_count": (C.c_longlong, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -346,12 +347,18 @@ def profile(enable: bool) -> None:
 
 
 def profile_read() -> dict:
-    """{category: (milliseconds, applications)} from the recorded CUDA events."""
+    """{category: (milliseconds, applications, systems)} from the recorded CUDA events."""
     n = len(PROF_NAMES)
     ms = np.zeros(n)
     cnt = np.zeros(n, np.int64)
-    _check(lib().csem_profile_read(n, _p(ms), cnt.ctypes.data_as(_lp)))
-    return {PROF_NAMES[i]: (float(ms[i]), int(cnt[i])) for i in range(n)}
+    units = np.zeros(n, np.int64)
+    _check(lib().csem_profile_read(n, _p(ms), cnt.ctypes.data_as(_lp), units.ctypes.data_as(_lp)))
+    return {PROF_NAMES[i]: (float(ms[i]), int(cnt[i]), int(units[i])) for i in range(n)}
+
+
+def launch_count() -> int:
+    """Kernel launches issued by libcsem_gpu.so so far (cuFFT's own kernels excluded)."""
+    return int(lib().csem_launch_count())
 
 
 def cdot(a, b, c64=False) -> complex:

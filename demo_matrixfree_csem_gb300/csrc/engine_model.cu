@@ -304,18 +304,18 @@ template <class P>
 void Ops<P>::zero(C* Y, long n, int nslot, const int* sys_list)
 {
   dim3 grd((unsigned)((n + 255) / 256), nslot);
-  k_zero_slots<C><<<grd, 256, 0, st>>>(Y, n, sys_list);
+  count_launch(), k_zero_slots<C><<<grd, 256, 0, st>>>(Y, n, sys_list);
 }
 
 template <class P>
 void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
 {
-  ProfScope whole(P::exact ? PROF_A64 : PROF_A32, st);
+  ProfScope whole(P::exact ? PROF_A64 : PROF_A32, st, nslot);
   const GridP<P>& g = m->grid<P>();
   if (m->airbc) {
     const AirP<P>& a = m->air<P>();
     {
-      ProfScope air(P::exact ? PROF_AIR64 : PROF_AIR32, st);
+      ProfScope air(P::exact ? PROF_AIR64 : PROF_AIR32, st, nslot);
       launch_hz0<P>(g, sc, X, hz0.as<C>(), nslot, sys_list, st);
       launch_air_gather<P>(a, hz0.as<C>(), K.as<C>(), nslot, st);
       fft->exec(P::exact, K.p, nslot, CUFFT_FORWARD, st);
@@ -323,10 +323,10 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
       fft->exec(P::exact, K2.p, 2 * nslot, CUFFT_INVERSE, st);
       launch_air_scatter<P>(a, K2.as<C>(), ghx.as<C>(), ghy.as<C>(), nslot, st);
     }
-    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st);
+    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
     launch_fdfd<P>(g, sc, X, Y, ghx.as<C>(), ghy.as<C>(), nslot, sys_list, st);
   } else {
-    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st);
+    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
     launch_fdfd<P>(g, sc, X, Y, nullptr, nullptr, nslot, sys_list, st);
   }
 }
@@ -334,7 +334,7 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
 template <class P>
 void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
 {
-  ProfScope prof(P::exact ? PROF_LUSGS64 : PROF_LUSGS32, st);
+  ProfScope prof(P::exact ? PROF_LUSGS64 : PROF_LUSGS32, st, nslot);
   SweepP<P> s;
   memset(&s, 0, sizeof(s));
   s.g = m->grid<P>();
@@ -366,7 +366,7 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
 template <class P>
 void Ops<P>::apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
 {
-  ProfScope prof(P::exact ? PROF_APHI64 : PROF_APHI32, st);
+  ProfScope prof(P::exact ? PROF_APHI64 : PROF_APHI32, st, nslot);
   if (!V.p) {
     V.alloc(sizeof(C) * (size_t)m->lv * nmax);
     BV.alloc(sizeof(C) * (size_t)m->lv * nmax);

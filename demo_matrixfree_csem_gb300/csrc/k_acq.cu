@@ -121,7 +121,7 @@ __global__ void k_extract(AcqGrid g, int nslot, int nch, const int* __restrict__
 void launch_inject(const AcqGrid& g, int nslot, const float* src, const double2* iom, const int* ch, int nch,
                    double2* B, cudaStream_t st)
 {
-  k_inject<<<(nslot + 31) / 32, 32, 0, st>>>(g, nslot, src, iom, ch, nch, B);
+  count_launch(), k_inject<<<(nslot + 31) / 32, 32, 0, st>>>(g, nslot, src, iom, ch, nch, B);
 }
 
 template <class C>
@@ -130,7 +130,7 @@ void launch_extract(const AcqGrid& g, int nslot, int nch, const int* ch, int nre
 {
   long n = (long)nslot * nch * nrec;
   if (n == 0) return;
-  k_extract<C><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, nslot, nch, ch, nrec, rec, X, xstride, sys_list, out);
+  count_launch(), k_extract<C><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g, nslot, nch, ch, nrec, rec, X, xstride, sys_list, out);
 }
 template void launch_extract<double2>(const AcqGrid&, int, int, const int*, int, const float*, const double2*, long,
                                       const int*, double2*, cudaStream_t);

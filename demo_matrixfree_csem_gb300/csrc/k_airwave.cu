@@ -93,7 +93,7 @@ template <class P>
 void launch_air_gather(const AirP<P>& a, const typename P::C* hz0, typename P::C* K, int nslot, cudaStream_t st)
 {
   dim3 grd((a.N1 + 127) / 128, a.N2, nslot);
-  k_air_gather<P><<<grd, 128, 0, st>>>(a, hz0, K);
+  count_launch(), k_air_gather<P><<<grd, 128, 0, st>>>(a, hz0, K);
 }
 
 template <class P>
@@ -101,7 +101,7 @@ void launch_air_filter(const AirP<P>& a, const typename P::C* K, typename P::C* 
 {
   long NN = (long)a.N1 * a.N2;
   dim3 grd((unsigned)((NN + 255) / 256), nslot);
-  k_air_filter<P><<<grd, 256, 0, st>>>(a, K, K2);
+  count_launch(), k_air_filter<P><<<grd, 256, 0, st>>>(a, K, K2);
 }
 
 template <class P>
@@ -109,7 +109,7 @@ void launch_air_scatter(const AirP<P>& a, const typename P::C* K2, typename P::C
                         int nslot, cudaStream_t st)
 {
   dim3 grd((a.n1 + 1 + 127) / 128, a.n2 + 1, nslot);
-  k_air_scatter<P><<<grd, 128, 0, st>>>(a, K2, ghx, ghy);
+  count_launch(), k_air_scatter<P><<<grd, 128, 0, st>>>(a, K2, ghx, ghy);
 }
 
 template void launch_air_gather<F64>(const AirP<F64>&, const double2*, double2*, int, cudaStream_t);

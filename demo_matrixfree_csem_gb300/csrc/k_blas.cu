@@ -128,8 +128,8 @@ void launch_dot(const typename P::C* a, const typename P::C* b, long n, long str
                 const int* sys_list, double2* partial, int nblk, double2* out, cudaStream_t st)
 {
   dim3 grd(nblk, nslot);
-  k_dot_partial<P><<<grd, DOT_THREADS, 0, st>>>(a, b, n, stride, sys_list, partial, nblk);
-  k_dot_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out);
+  count_launch(), k_dot_partial<P><<<grd, DOT_THREADS, 0, st>>>(a, b, n, stride, sys_list, partial, nblk);
+  count_launch(), k_dot_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out);
 }
 
 template void launch_dot<F64>(const double2*, const double2*, long, long, int, const int*, double2*, int,
@@ -240,12 +240,12 @@ void launch_vec(int op, long n, int nslot, const int* sys_list, const KrylovScal
 {
   dim3 grd((unsigned)((n + 255) / 256), nslot);
   switch (op) {
-  case VEC_INIT: k_vec_init<P><<<grd, 256, 0, st>>>(n, sys_list, a, b, c, d, e); break;
-  case VEC_S: k_vec_s<P><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c); break;
-  case VEC_XR: k_vec_xr<P, false><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c, d, e); break;
-  case VEC_SUB: k_vec_sub<P><<<grd, 256, 0, st>>>(n, sys_list, a, b, c); break;
-  case VEC_XR_PLAIN: k_vec_xr<P, true><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c, d, e); break;
-  case VEC_P: k_vec_p<P><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c); break;
+  case VEC_INIT: count_launch(), k_vec_init<P><<<grd, 256, 0, st>>>(n, sys_list, a, b, c, d, e); break;
+  case VEC_S: count_launch(), k_vec_s<P><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c); break;
+  case VEC_XR: count_launch(), k_vec_xr<P, false><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c, d, e); break;
+  case VEC_SUB: count_launch(), k_vec_sub<P><<<grd, 256, 0, st>>>(n, sys_list, a, b, c); break;
+  case VEC_XR_PLAIN: count_launch(), k_vec_xr<P, true><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c, d, e); break;
+  case VEC_P: count_launch(), k_vec_p<P><<<grd, 256, 0, st>>>(n, sys_list, ks, a, b, c); break;
   }
 }
 
@@ -254,7 +254,7 @@ void launch_axpy(long n, int nslot, const int* sys_list, const double2* coef, in
                  const typename P::C* x, typename P::C* y, cudaStream_t st)
 {
   dim3 grd((unsigned)((n + 255) / 256), nslot);
-  k_vec_axpy<P><<<grd, 256, 0, st>>>(n, sys_list, coef, coef_stride, neg, x, y);
+  count_launch(), k_vec_axpy<P><<<grd, 256, 0, st>>>(n, sys_list, coef, coef_stride, neg, x, y);
 }
 
 template <class P>
@@ -262,7 +262,7 @@ void launch_cdivv(long n, int nslot, const int* sys_list, const double2* d, int 
                   const typename P::C* x, typename P::C* y, cudaStream_t st)
 {
   dim3 grd((unsigned)((n + 255) / 256), nslot);
-  k_vec_cdiv<P><<<grd, 256, 0, st>>>(n, sys_list, d, dstride, real_only, x, y);
+  count_launch(), k_vec_cdiv<P><<<grd, 256, 0, st>>>(n, sys_list, d, dstride, real_only, x, y);
 }
 
 #define CSEM_INST(P)                                                                                        \

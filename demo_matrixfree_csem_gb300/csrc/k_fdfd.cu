@@ -160,7 +160,7 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
   int kchunk = (g.n3 + 1 + nkc - 1) / nkc;
   nkc = (g.n3 + 1 + kchunk - 1) / kchunk;
   dim3 grd(gx, gy, nsys * nkc);
-  k_fdfd<P, BX, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
+  count_launch(), k_fdfd<P, BX, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
 }
 
 template <class P>
@@ -169,7 +169,7 @@ void launch_hz0(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* 
 {
   dim3 blk(32, 8);
   dim3 grd((g.n1 + 31) / 32, (g.n2 + 7) / 8, nsys);
-  k_hz0<P><<<grd, blk, 0, st>>>(g, scal, X, out, sys_list);
+  count_launch(), k_hz0<P><<<grd, blk, 0, st>>>(g, scal, X, out, sys_list);
 }
 
 template void launch_fdfd<F64>(const GridP<F64>&, const SysScal<F64>*, const double2*, double2*,

@@ -228,7 +228,7 @@ void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int 
   if (len <= 0) return;
   dim3 blk(32, 4);
   dim3 grd((cN + 31) / 32, (len + 3) / 4, nslot);
-#define CSEM_SW(C, F, A) k_sweep<P, C, F, A><<<grd, blk, 0, st>>>(s, t)
+#define CSEM_SW(C, F, A) count_launch(), k_sweep<P, C, F, A><<<grd, blk, 0, st>>>(s, t)
   if (!aphi) {
     if (comp == 0) { if (fwd) CSEM_SW(0, true, false); else CSEM_SW(0, false, false); }
     else if (comp == 1) { if (fwd) CSEM_SW(1, true, false); else CSEM_SW(1, false, false); }
@@ -352,7 +352,7 @@ template <class P>
 void launch_aphi_div(const SweepP<P>& s, typename P::C* BV, int nslot, cudaStream_t st)
 {
   dim3 grd((unsigned)((s.lv + 255) / 256), 1, nslot);
-  k_aphi_div<P><<<grd, 256, 0, st>>>(s, BV);
+  count_launch(), k_aphi_div<P><<<grd, 256, 0, st>>>(s, BV);
 }
 
 template <class P>
@@ -361,15 +361,15 @@ void launch_aphi_phi(const SweepP<P>& s, typename P::C* V, int t, int nslot, cud
   // t > 0: forward hyperplane t; t < 0: backward hyperplane -t
   dim3 blk(32, 4);
   dim3 grd((s.g.n1 - 1 + 31) / 32, (s.g.n2 - 1 + 3) / 4, nslot);
-  if (t > 0) k_aphi_phi<P, true><<<grd, blk, 0, st>>>(s, V, t);
-  else k_aphi_phi<P, false><<<grd, blk, 0, st>>>(s, V, -t);
+  if (t > 0) count_launch(), k_aphi_phi<P, true><<<grd, blk, 0, st>>>(s, V, t);
+  else count_launch(), k_aphi_phi<P, false><<<grd, blk, 0, st>>>(s, V, -t);
 }
 
 template <class P>
 void launch_aphi_grad(const SweepP<P>& s, const typename P::C* V, int nslot, cudaStream_t st)
 {
   dim3 grd((unsigned)((s.g.lE + 255) / 256), 1, nslot);
-  k_aphi_grad<P><<<grd, 256, 0, st>>>(s, V);
+  count_launch(), k_aphi_grad<P><<<grd, 256, 0, st>>>(s, V);
 }
 
 #define CSEM_INST(P)                                                                              \

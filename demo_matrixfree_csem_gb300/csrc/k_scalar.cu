@@ -91,21 +91,21 @@ static inline dim3 nb32(int n) { return dim3((n + 31) / 32); }
 void launch_sc_init(int nslot, const int* sys_list, KrylovScalars* ks, const double2* d_rr0, const double2* d_rr,
                     double* hist, int hist_cap, cudaStream_t st)
 {
-  k_sc_init<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_rr0, d_rr, hist, hist_cap);
+  count_launch(), k_sc_init<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_rr0, d_rr, hist, hist_cap);
 }
 void launch_sc_alpha(int nslot, const int* sys_list, KrylovScalars* ks, const double2* d_vr0, cudaStream_t st)
 {
-  k_sc_alpha<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_vr0);
+  count_launch(), k_sc_alpha<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_vr0);
 }
 void launch_sc_omega(int nslot, const int* sys_list, KrylovScalars* ks, const double2* d_st, const double2* d_tt,
                      cudaStream_t st)
 {
-  k_sc_omega<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_st, d_tt);
+  count_launch(), k_sc_omega<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_st, d_tt);
 }
 void launch_sc_rs_beta(int nslot, const int* sys_list, KrylovScalars* ks, const double2* d_rr, const double2* d_rr0,
                        double* hist, int hist_cap, int maxiter, cudaStream_t st)
 {
-  k_sc_rs_beta<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_rr, d_rr0, hist, hist_cap, maxiter);
+  count_launch(), k_sc_rs_beta<<<nb32(nslot), 32, 0, st>>>(nslot, sys_list, ks, d_rr, d_rr0, hist, hist_cap, maxiter);
 }
 
 }  // namespace csem

@@ -7,7 +7,7 @@ namespace csem {
 
 namespace {
 struct Rec {
-  int cat;
+  int cat, units;
   cudaEvent_t a, b;
   bool closed;
 };
@@ -28,12 +28,16 @@ cudaEvent_t get_event()
 }
 }  // namespace
 
+static long long g_launches = 0;
+void count_launch(int n) { g_launches += n; }
+
 bool prof_on() { return g_on; }
 
-int prof_begin(int cat, cudaStream_t st)
+int prof_begin(int cat, cudaStream_t st, int units)
 {
   Rec r;
   r.cat = cat;
+  r.units = units;
   r.a = get_event();
   r.b = get_event();
   r.closed = false;
@@ -67,14 +71,19 @@ int csem_profile(int enable)
   return CSEM_OK;
 }
 
-/* ms[cat] = summed device milliseconds, count[cat] = applications, cat < ncat. */
-int csem_profile_read(int ncat, double* ms, long* count)
+/* Kernel launches issued by this library since it was loaded. */
+long long csem_launch_count(void) { return csem::g_launches; }
+
+/* ms[cat] = summed device milliseconds, count[cat] = applications, units[cat] =
+ * systems processed summed over applications; cat < ncat. */
+int csem_profile_read(int ncat, double* ms, long* count, long* units)
 {
   using namespace csem;
   cudaDeviceSynchronize();
   for (int c = 0; c < ncat; c++) {
     ms[c] = 0;
     count[c] = 0;
+    if (units) units[c] = 0;
   }
   for (auto& r : g_recs) {
     if (!r.closed || r.cat >= ncat) continue;
@@ -82,6 +91,7 @@ int csem_profile_read(int ncat, double* ms, long* count)
     if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
       ms[r.cat] += t;
       count[r.cat] += 1;
+      if (units) units[r.cat] += r.units;
     }
   }
   return CSEM_OK;

@@ -10,14 +10,18 @@ enum ProfCat {
   PROF_AIR64 = 6, PROF_AIR32 = 7, PROF_STENCIL64 = 8, PROF_STENCIL32 = 9, PROF_NCAT = 16
 };
 
+// count of this library's kernel launches (cuFFT's own kernels excluded)
+void count_launch(int n = 1);
+
 bool prof_on();
-int prof_begin(int cat, cudaStream_t st);   // returns a token (-1 when off)
+int prof_begin(int cat, cudaStream_t st, int units);   // returns a token (-1 when off)
 void prof_end(int token, cudaStream_t st);
 
+// `units` = systems processed by this application (for bytes-per-application figures)
 struct ProfScope {
   int tok;
   cudaStream_t st;
-  ProfScope(int cat, cudaStream_t s) : tok(prof_on() ? prof_begin(cat, s) : -1), st(s) {}
+  ProfScope(int cat, cudaStream_t s, int units) : tok(prof_on() ? prof_begin(cat, s, units) : -1), st(s) {}
   ~ProfScope() { if (tok >= 0) prof_end(tok, st); }
 };
 

@@ -157,12 +157,16 @@ int Solver64::fbicgstab(int precond, int mp, double2* x, const double2* b, int n
 
 void Solver64::gmres_pre(int mp, const double2* b, double2* x)
 {
-  // fixed mp-step GMRES on A from x = 0 (gmres_init_free.c:58-137); vectors after the
-  // outer solver's: w, r, V[0..mp]
-  const int base = 7 + 24;
-  ensure_work(base + mp + 3);
-  double2 *w = W(base), *r = W(base + 1);
-  auto V = [&](int i) { return W(base + 2 + i); };
+  // fixed mp-step GMRES on A from x = 0 (gmres_init_free.c:58-137); its vectors
+  // w, r, V[0..mp] live in a buffer of their own, so growing it never moves the outer
+  // solver's vectors
+  if (pre_mp < mp) {
+    prework.alloc(sizeof(double2) * (size_t)n * (mp + 3));
+    pre_mp = mp;
+  }
+  double2* pw = prework.as<double2>();
+  double2 *w = pw, *r = pw + n;
+  auto V = [&](int i) { return pw + (size_t)(2 + i) * n; };
   std::vector<hz> h((size_t)(mp + 1) * mp, H(0, 0)), g(mp + 1, H(0, 0)), yv(mp + 1), c(mp + 1);
   std::vector<double> sn(mp + 1, 0.0);
   auto Hm = [&](int i, int j) -> hz& { return h[(size_t)i * mp + j]; };

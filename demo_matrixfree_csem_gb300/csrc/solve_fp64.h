@@ -13,8 +13,8 @@ class Solver64 {
   Ops<F64> ops;
   long n;
   int nblk;
-  DevBuf scal, ks, dots, partial, coef, hist, work;
-  int nwork = 0;
+  DevBuf scal, ks, dots, partial, coef, hist, work, prework;
+  int nwork = 0, pre_mp = 0;
   void set_iom(double re, double im);
   double2* W(int i);
   void ensure_work(int count);

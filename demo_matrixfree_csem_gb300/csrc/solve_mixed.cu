@@ -129,7 +129,7 @@ void MixedBatch::start_inner(const std::vector<int>& g, const std::vector<double
   const int ng = (int)g.size();
   const int* dl = list.as<int>();
   dim3 grd((unsigned)((n + 255) / 256), ng);
-  k_start_inner<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), r64.as<double2>(), V(0), V(1), V(2), V(7));
+  count_launch(), k_start_inner<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), r64.as<double2>(), V(0), V(1), V(2), V(7));
   double2* D = dots.as<double2>();
   launch_dot<F32>(V(0), V(1), n, n, ng, dl, partial.as<double2>(), nblk, D + 5 * nsys, st);
   launch_dot<F32>(V(0), V(0), n, n, ng, dl, partial.as<double2>(), nblk, D + 6 * nsys, st);
@@ -144,7 +144,7 @@ void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rn
   const int* dl = list.as<int>();
   dim3 grd((unsigned)((n + 255) / 256), ng);
   if (!first) {
-    k_outer_accum<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), x64.as<double2>(), V(7));
+    count_launch(), k_outer_accum<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), x64.as<double2>(), V(7));
     o64.apply_A(x64.as<double2>(), w64.as<double2>(), ng, dl, sc64.as<SysScal<F64>>());
     launch_vec<F64>(VEC_SUB, n, ng, dl, nullptr, b64.as<double2>(), w64.as<double2>(), r64.as<double2>(), nullptr,
                     nullptr, st);

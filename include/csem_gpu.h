@@ -145,7 +145,11 @@ int csem_ctx_sync(csem_ctx *c);
  * 2/3 LU-SGS, 4/5 A-phi, 6/7 airwave only, 8/9 stencil kernel only.
  * csem_profile(1) clears and starts recording, csem_profile(0) stops. */
 int csem_profile(int enable);
-int csem_profile_read(int ncat, double *ms, long *count);
+/* ms: summed device milliseconds, count: applications, units (may be NULL): systems
+ * processed summed over the applications */
+int csem_profile_read(int ncat, double *ms, long *count, long *units);
+/* kernel launches issued by this library since it was loaded (cuFFT's excluded) */
+long long csem_launch_count(void);
 
 #ifdef __cplusplus
 }
