@@ -85,6 +85,7 @@ def lib(build_if_missing: bool = True):
         "csem_ctx_destroy": (None, [C.c_void_p]),
         "csem_ctx_sizes": (C.c_int, [C.c_void_p, _lp]),
         "csem_ctx_sync": (C.c_int, [C.c_void_p]),
+        "csem_ctx_stream": (C.c_void_p, [C.c_void_p]),
         "csem_fdfd_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_lusgs_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_aphi_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -231,6 +232,11 @@ class Ctx:
         _check(lib().csem_ctx_sizes(self.h, s))
         (self.lE, self.lEx, self.lEy, self.lEz, self.lv, self.n1, self.n2, self.n3, self.n3f, self.nb) = list(s)
         self.airbc, self.fvm = airbc, fvm
+
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(lib().csem_ctx_stream(self.h) or 0)
 
     def close(self):
         if getattr(self, "h", None) and _LIB is not None:

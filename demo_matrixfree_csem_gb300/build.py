@@ -18,6 +18,7 @@ HOST = os.path.join(PKG, "host")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libcsem_gpu.so")
 DRIVER = os.path.join(OUT, "csem")
+REFABI = os.path.join(OUT, "libcsem_refabi.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -95,6 +96,10 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         _run(["g++", "-shared", "-o", tmp, *objs, f"-L{cuda_lib}", "-lcufft", "-lcudart",
               f"-Wl,-rpath,{cuda_lib}"], verbose)
         os.replace(tmp, LIB)
+    refabi_src = os.path.join(HOST, "csem_refabi.c")
+    if force or _newer(REFABI, [refabi_src, LIB] + hdrs):
+        _run(["gcc", "-O3", "-fPIC", "-ffp-contract=off", "-std=gnu99", "-Wall", "-shared", "-I", INCLUDE, refabi_src,
+              "-o", REFABI, f"-L{OUT}", "-lcsem_gpu", f"-Wl,-rpath,{OUT}"], verbose)
     drv_src = [os.path.join(HOST, s) for s in DRIVER_SOURCES]
     if all(os.path.exists(s) for s in drv_src) and (force or _newer(DRIVER, drv_src + [LIB] + hdrs)):
         _run(["gcc", "-O3", "-ffp-contract=off", "-std=gnu99", "-Wall", "-I", INCLUDE, *drv_src, "-o", DRIVER,

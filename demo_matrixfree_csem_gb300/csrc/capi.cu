@@ -131,6 +131,8 @@ int csem_ctx_sizes(const csem_ctx* c, long* o)
   return CSEM_OK;
 }
 
+void* csem_ctx_stream(csem_ctx* c) { return (void*)c->st; }
+
 int csem_ctx_sync(csem_ctx* c)
 {
   API_BEGIN

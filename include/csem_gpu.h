@@ -137,6 +137,8 @@ int csem_aphi_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, cons
 int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
 /* synchronise the context's stream */
 int csem_ctx_sync(csem_ctx *c);
+/* the context's CUDA stream (a cudaStream_t), for callers that record events on it */
+void *csem_ctx_stream(csem_ctx *c);
 
 /* ------------------------------------------------------------ timing
  * Per-operator device time from CUDA events recorded on the operator's stream around
