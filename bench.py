@@ -163,6 +163,31 @@ def cpu_baseline(workload: str, freqs, processes: int, iters: int):
                        f"published Marlim iteration counts (mean {its:.0f} iterations per solve)")}
 
 
+# ----------------------------------------------------------------------------- ranks
+def wave_systems(cfg, systems, wave, k, rank):
+    """Frequencies and source positions of step k on `rank`. Steps walk the system list
+    in waves of `wave`; every rank owns its own sources (rank r's are shifted by 50 m * r
+    along y), so the units of different ranks are disjoint and no data is exchanged
+    (weak scaling)."""
+    nwaves = (len(systems) + wave - 1) // wave
+    w = k % nwaves
+    sel = systems[w * wave:(w + 1) * wave]
+    f = np.array([s[0] for s in sel], np.float32)
+    src = np.stack([cfg.acq.src[s[1], :3] for s in sel]).astype(np.float32)
+    src[:, 1] += 50.0 * rank
+    return f, src
+
+
+def max_over_ranks(values, device):
+    """Element-wise maximum over all ranks of a list of floats (the timed region of the
+    slowest rank)."""
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 # ----------------------------------------------------------------------------- GPU leg
 def run_ours(args):
     import demo_matrixfree_csem_gb300 as cs
@@ -182,16 +207,9 @@ def run_ours(args):
     ctx = cs.Ctx(G, int(cfg.params["airbc"]), 0)
     rec = cfg.acq.rec
     wave = args.wave
-    nwaves = (len(systems) + wave - 1) // wave
 
     def step_systems(k):
-        w = k % nwaves
-        sel = systems[w * wave:(w + 1) * wave]
-        f = np.array([s[0] for s in sel], np.float32)
-        src = np.stack([cfg.acq.src[s[1], :3] for s in sel]).astype(np.float32)
-        if rank:  # weak scaling: every rank owns its own sources (shifted along y)
-            src[:, 1] += 50.0 * rank
-        return f, src
+        return wave_systems(cfg, systems, wave, k, rank)
 
     opts = dict(rec=rec, precision=32, preco=1, niter=1000, tol=1e-8, inner_tol=args.inner_tol,
                 check_every=args.check_every)
@@ -242,9 +260,7 @@ def run_ours(args):
     cs.profile(False)
     ck = clocks.stop()
     if dist:
-        t = torch.tensor([wall, dev_ms / 1e3], device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        wall, dev_s = float(t[0]), float(t[1])
+        wall, dev_s = max_over_ranks([wall, dev_ms / 1e3], "cuda")
         nsolved *= world
     else:
         dev_s = dev_ms / 1e3
@@ -304,9 +320,6 @@ def main():
             return
         cfg, freqs, systems = make_workload(args.workload, tmp)
         ncores = os.cpu_count() or 1
-        steps = []
-        for _ in range(args.warmup + args.steps):
-            pass
         cb = cpu_baseline(args.workload, freqs, ncores, args.cpu_iters)
         line = {"impl": "reference", "metric": metric, "value": cb["value"], "unit": "solves/s",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -320,7 +333,6 @@ def main():
     res, cfg, freqs, systems = run_ours(args)
     if rank != 0:
         return
-    res["sys_iters_launched"] = sum(res["iters"])
     value = res["nsolved"] / res["dev_s"]
     e2e = res["nsolved"] / res["wall"]
     dom, rf = roofline(res, peaks)

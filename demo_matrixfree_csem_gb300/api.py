@@ -86,6 +86,7 @@ def lib(build_if_missing: bool = True):
         "csem_ctx_sizes": (C.c_int, [C.c_void_p, _lp]),
         "csem_ctx_sync": (C.c_int, [C.c_void_p]),
         "csem_ctx_stream": (C.c_void_p, [C.c_void_p]),
+        "csem_ctx_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
         "csem_fdfd_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_lusgs_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_aphi_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -232,6 +233,10 @@ class Ctx:
         _check(lib().csem_ctx_sizes(self.h, s))
         (self.lE, self.lEx, self.lEy, self.lEz, self.lv, self.n1, self.n2, self.n3, self.n3f, self.nb) = list(s)
         self.airbc, self.fvm = airbc, fvm
+
+    def set_option(self, name: str, value: int) -> None:
+        """Kernel-schedule options, e.g. set_option("lusgs_pipelined", 0)."""
+        _check(lib().csem_ctx_set_option(self.h, name.encode(), int(value)))
 
     @property
     def stream(self) -> int:

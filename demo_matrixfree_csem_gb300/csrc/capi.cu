@@ -22,6 +22,7 @@ struct csem_ctx {
   MixedBatch* batch = nullptr;
   DevBuf io[4], sc64, sc32, dotp;
   int nmax64 = 0, nmax32 = 0;
+  bool lusgs_pipelined = true;
 };
 
 #define API_BEGIN try {
@@ -41,6 +42,7 @@ static Ops<F64>* ops64_for(csem_ctx* c, int nsys)
   if (!c->ops64 || c->nmax64 < nsys) {
     delete c->ops64;
     c->ops64 = new Ops<F64>(c->model, nsys, c->st);
+    c->ops64->pipelined_sweeps = c->lusgs_pipelined;
     c->nmax64 = nsys;
   }
   return c->ops64;
@@ -51,6 +53,7 @@ static Ops<F32>* ops32_for(csem_ctx* c, int nsys)
   if (!c->ops32 || c->nmax32 < nsys) {
     delete c->ops32;
     c->ops32 = new Ops<F32>(c->model, nsys, c->st);
+    c->ops32->pipelined_sweeps = c->lusgs_pipelined;
     c->nmax32 = nsys;
   }
   return c->ops32;
@@ -132,6 +135,22 @@ int csem_ctx_sizes(const csem_ctx* c, long* o)
 }
 
 void* csem_ctx_stream(csem_ctx* c) { return (void*)c->st; }
+
+int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
+{
+  if (!strcmp(name, "lusgs_pipelined")) {
+    c->lusgs_pipelined = value != 0;
+    if (c->ops64) c->ops64->pipelined_sweeps = c->lusgs_pipelined;
+    if (c->ops32) c->ops32->pipelined_sweeps = c->lusgs_pipelined;
+    if (c->solver) c->solver->ops.pipelined_sweeps = c->lusgs_pipelined;
+    if (c->batch) {
+      c->batch->o64.pipelined_sweeps = c->lusgs_pipelined;
+      c->batch->o32.pipelined_sweeps = c->lusgs_pipelined;
+    }
+    return CSEM_OK;
+  }
+  return csem_set_error(CSEM_EINVAL, "unknown option %s", name);
+}
 
 int csem_ctx_sync(csem_ctx* c)
 {
@@ -225,7 +244,10 @@ int csem_aphi_apply_c64_host(csem_ctx* c, double re, double im, const float* x, 
 
 static Solver64* solver_for(csem_ctx* c)
 {
-  if (!c->solver) c->solver = new Solver64(c->model, c->st);
+  if (!c->solver) {
+    c->solver = new Solver64(c->model, c->st);
+    c->solver->ops.pipelined_sweeps = c->lusgs_pipelined;
+  }
   return c->solver;
 }
 
@@ -362,6 +384,8 @@ static MixedBatch* batch_for(csem_ctx* c, int nsys)
     delete c->batch;
     c->batch = nullptr;
     c->batch = new MixedBatch(c->model, nsys, c->st);
+    c->batch->o64.pipelined_sweeps = c->lusgs_pipelined;
+    c->batch->o32.pipelined_sweeps = c->lusgs_pipelined;
   }
   return c->batch;
 }

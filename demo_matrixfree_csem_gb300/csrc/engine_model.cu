@@ -353,6 +353,11 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
     CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, sizeof(C) * (size_t)s.capE * nslot, st));
   }
   zero(Y, m->lE, nslot, sys_list);
+  if (pipelined_sweeps) {
+    for (int comp = 0; comp < 3; comp++) launch_sweep_pipelined<P>(s, comp, true, nslot, st);
+    for (int comp = 2; comp >= 0; comp--) launch_sweep_pipelined<P>(s, comp, false, nslot, st);
+    return;
+  }
   for (int comp = 0; comp < 3; comp++) {
     const int nd = sweep_diagonals(comp, n1, n2, s.nK);
     for (int t = 2; t < 2 + nd; t++) launch_sweep<P>(s, comp, true, false, t, nslot, st);

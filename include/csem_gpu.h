@@ -139,6 +139,10 @@ int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, doub
 int csem_ctx_sync(csem_ctx *c);
 /* the context's CUDA stream (a cudaStream_t), for callers that record events on it */
 void *csem_ctx_stream(csem_ctx *c);
+/* Kernel-schedule options (results do not depend on them):
+ *   "lusgs_pipelined" 1 (default): one pipelined-warp launch per LU-SGS component sweep;
+ *                     0: one launch per wavefront diagonal. */
+int csem_ctx_set_option(csem_ctx *c, const char *name, int value);
 
 /* ------------------------------------------------------------ timing
  * Per-operator device time from CUDA events recorded on the operator's stream around

@@ -8,7 +8,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-GOLDEN_CASES = sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)))
+# per-operator cases (args.json + golden.npz); layered_120/ holds whole-solve receivers only
+GOLDEN_CASES = sorted(d for d in os.listdir(GOLDEN) if os.path.exists(os.path.join(GOLDEN, d, "args.json")))
 
 
 def parse_args(args: list[str]) -> dict:

@@ -1,0 +1,70 @@
+"""Whole solves of the layered 120^3 workload against the reference's own receivers.
+
+The fixture tests/golden/layered_120/reference_receivers.npz was computed by the
+reference itself (built from its sources, FFTW replaced by the oracle's DFT) with
+BiCGStab + LU-SGS to tol = 1e-8/f at 0.25, 0.75 and 1.25 Hz. Errors are max-norm
+relative per frequency and channel. Ey is zero by symmetry on the receiver line (its
+values are rounding noise, about 1e-8 of Ex), so Ey is measured against the Ex max.
+
+Bounds:
+  * complex128 GPU drop-in (injection, solve, extraction through the C ABI): Ex, Ez
+    <= 5e-9 (the two runs differ only in dot-product summation order and in the
+    airwave FFT's rounding, which BiCGStab amplifies over hundreds of iterations);
+    iteration counts within 15%; the first 20 residuals within 2e-6 relative (the reference prints 7 digits);
+  * batched mixed precision (complex64 inner, complex128 defect correction): <= 1e-7.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import demo_matrixfree_csem_gb300 as cs
+from cases import product_grid
+from demo_matrixfree_csem_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+FIX = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "layered_120", "reference_receivers.npz")
+
+
+@pytest.fixture(scope="module")
+def layered(tmp_path_factory):
+    d = str(tmp_path_factory.mktemp("layered"))
+    cfg = synthetic.layered_120()
+    synthetic.write_config(cfg, d)
+    p = {k: str(v) for k, v in cfg.params.items()}
+    G = product_grid(d, p)
+    return cfg, cs.Ctx(G, 1, 0), np.load(FIX)
+
+
+def _errors(dcal, ref):
+    ex = np.abs(ref[0]).max()
+    return [float(np.abs(dcal[c] - ref[c]).max() / (np.abs(ref[c]).max() if c != 1 else ex)) for c in range(3)]
+
+
+def test_fp64_dropin_matches_reference(gpu, layered):
+    cfg, ctx, z = layered
+    src = cfg.acq.src[0]
+    for f in range(3):
+        freq = float(z["freqs"][f])
+        iom = cs.iom_of(freq)
+        b = ctx.inject_source(iom, ["Ex"], src)
+        tol = float(np.float32(np.float32(1e-8) / np.float32(freq)))
+        x, hist, it, st = ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=1000, tol=tol)
+        assert st == "converged"
+        err = _errors(ctx.extract_emf(["Ex", "Ey", "Ez"], cfg.acq.rec, x), z["rec"][f])
+        assert max(err) <= 5e-9, (freq, err)
+        href = z[f"hist{f}"]
+        assert abs(it - (len(href) - 1)) <= 0.15 * (len(href) - 1), (freq, it, len(href) - 1)
+        np.testing.assert_allclose(hist[:20], href[:20], rtol=2e-6)
+
+
+def test_mixed_batch_matches_reference(gpu, layered):
+    cfg, ctx, z = layered
+    freqs = np.asarray(z["freqs"], np.float32)
+    src = np.repeat(cfg.acq.src[:1, :3], 3, axis=0)
+    r = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=32, preco=1, niter=1000, tol=1e-8)
+    assert r["status"] == ["converged"] * 3, r["status"]
+    for f in range(3):
+        err = _errors(r["dcal"][f], z["rec"][f])
+        assert max(err) <= 1e-7, (float(freqs[f]), err)

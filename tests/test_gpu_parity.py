@@ -119,7 +119,15 @@ def test_larger_grid_bit_exact(gpu, tmp_path, airbc, fvm):
         assert relerr(ya, yo) <= 1e-12
     else:
         assert np.array_equal(ya, yo)
-    assert np.array_equal(ctx.lusgs_apply(iom, x), O.lusgs(x))
+    mo = O.lusgs(x)
+    for sched in (1, 0):  # pipelined warps and one launch per diagonal: same order, same bits
+        ctx.set_option("lusgs_pipelined", sched)
+        assert np.array_equal(ctx.lusgs_apply(iom, x), mo), sched
+    ctx.set_option("lusgs_pipelined", 0)
+    m32_diag = ctx.lusgs_apply(iom, x, c64=True)
+    ctx.set_option("lusgs_pipelined", 1)
+    m32_pipe = ctx.lusgs_apply(iom, x, c64=True)
+    assert relerr(m32_pipe, mo) <= 2e-5 and relerr(m32_diag, mo) <= 2e-5
 
 
 @pytest.mark.parametrize("airbc", [0, 1])
