@@ -211,7 +211,7 @@ def run_ours(args):
     def step_systems(k):
         return wave_systems(cfg, systems, wave, k, rank)
 
-    opts = dict(rec=rec, precision=32, preco=1, niter=1000, tol=1e-8, inner_tol=args.inner_tol,
+    opts = dict(rec=rec, precision=32, preco=1, niter=args.niter, tol=1e-8, inner_tol=args.inner_tol,
                 check_every=args.check_every)
     # pinned host staging for the e2e leg
     pin = {}
@@ -306,6 +306,9 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=1e-4)
     ap.add_argument("--check-every", type=int, default=4)
     ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--niter", type=int, default=1000,
+                    help="inner iteration budget per system (the reference's niter); lower values are for "
+                         "profiling runs, whose systems then stop unconverged")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))

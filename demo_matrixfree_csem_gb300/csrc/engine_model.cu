@@ -353,19 +353,21 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
     CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, sizeof(C) * (size_t)s.capE * nslot, st));
   }
   zero(Y, m->lE, nslot, sys_list);
-  if (pipelined_sweeps) {
-    for (int comp = 0; comp < 3; comp++) launch_sweep_pipelined<P>(s, comp, true, nslot, st);
-    for (int comp = 2; comp >= 0; comp--) launch_sweep_pipelined<P>(s, comp, false, nslot, st);
-    return;
-  }
-  for (int comp = 0; comp < 3; comp++) {
+  // both schedules visit the points of a sweep in an order that respects every
+  // dependency of the lexicographic sweep, so they may be mixed sweep by sweep
+  auto sweep = [&](int comp, bool fwd) {
+    if (pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
+      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st);
+      return;
+    }
     const int nd = sweep_diagonals(comp, n1, n2, s.nK);
-    for (int t = 2; t < 2 + nd; t++) launch_sweep<P>(s, comp, true, false, t, nslot, st);
-  }
-  for (int comp = 2; comp >= 0; comp--) {
-    const int nd = sweep_diagonals(comp, n1, n2, s.nK);
-    for (int t = 1 + nd; t >= 2; t--) launch_sweep<P>(s, comp, false, false, t, nslot, st);
-  }
+    if (fwd)
+      for (int t = 2; t < 2 + nd; t++) launch_sweep<P>(s, comp, true, false, t, nslot, st);
+    else
+      for (int t = 1 + nd; t >= 2; t--) launch_sweep<P>(s, comp, false, false, t, nslot, st);
+  };
+  for (int comp = 0; comp < 3; comp++) sweep(comp, true);
+  for (int comp = 2; comp >= 0; comp--) sweep(comp, false);
 }
 
 template <class P>

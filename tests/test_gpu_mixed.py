@@ -59,7 +59,7 @@ def test_fp64_batch_matches_oracle(gpu, small_case):
         for c in range(3):
             bound = min(1e-6, max(1e-9, 100 * relerr(ref1[c], ref[c])))
             assert relerr(r64["dcal"][s, c], ref[c]) <= bound, (s, c, bound)
-        assert abs(r64["iters"][s] - it) <= max(2, 0.05 * it)
+        assert abs(r64["iters"][s] - it) <= max(2, 0.15 * it)
 
 
 def test_mixed_batch_matches_fp64(gpu, small_case):
