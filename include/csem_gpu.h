@@ -135,6 +135,21 @@ int csem_lusgs_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, con
 int csem_aphi_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
 /* out[s] (complex128, device) = <a_s, b_s> for nsys vectors of length n (stride n) */
 int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
+/* The same dot products, identical bits, without any device allocation by the library.
+ * No counterpart in the reference (its cdotprod, cdotprod.c:13-19, is a host loop).
+ * For callers that cannot let a library allocate: one that has handed all free device
+ * memory to its own pool, or a loop that cannot absorb the device-wide synchronisation
+ * cudaMalloc/cudaFree may bring. csem_cdot_dev allocates its partial-sum buffer on first
+ * use; this variant keeps the partials in a fixed 1 MiB array inside the library's
+ * device image instead.
+ *  - nsys <= CSEM_NOALLOC_DOT_MAX_SYSTEMS, else CSEM_ETOOBIG with a message;
+ *  - the first call on a device (made with that device current) looks the array up with
+ *    cudaGetSymbolAddress and caches it: make that call before any stream capture starts;
+ *  - the array is shared by all calls on a device: calls that overlap in time (other
+ *    streams, other host threads) race on it; serialise them;
+ *  - nothing needs clearing beforehand: each call writes every partial it reads. */
+#define CSEM_NOALLOC_DOT_MAX_SYSTEMS 64
+int csem_cdot_dev_noalloc(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
 /* synchronise the context's stream */
 int csem_ctx_sync(csem_ctx *c);
 /* the context's CUDA stream (a cudaStream_t), for callers that record events on it */
