@@ -48,14 +48,10 @@ def log(*a):
 # ----------------------------------------------------------------------------- workload
 def make_workload(name: str, tmp: str):
     from demo_matrixfree_csem_gb300 import synthetic as syn
-    if name == "marlim_like_96":
-        cfg = syn.marlim_like(seed=0)
-    elif name == "layered_120":
-        cfg = syn.layered_120()
-    elif name == "vti_block_120":
-        cfg = syn.vti_block_120()
-    else:
-        raise SystemExit(f"unknown workload {name}")
+    try:
+        cfg = syn.workload(name)
+    except ValueError as e:
+        raise SystemExit(str(e))
     syn.write_config(cfg, tmp)
     freqs = [float(f) for f in cfg.params["freqs"].split(",")]
     systems = [(f, s) for f in freqs for s in range(len(cfg.acq.src))]
@@ -63,13 +59,8 @@ def make_workload(name: str, tmp: str):
 
 
 def grid_for(cfg, d):
-    import demo_matrixfree_csem_gb300 as cs
-    p = cfg.params
-    G = cs.Grid.from_files(*[os.path.join(d, n) for n in ("fx1", "fx2", "fx3", "frho11", "frho22", "frho33")])
-    G.extend(int(p["nb"]), float(p.get("lextend", -1)), 1e6, 1)
-    if int(p["airbc"]):
-        G.airbc(1024, 1024)
-    return G
+    from demo_matrixfree_csem_gb300 import synthetic as syn
+    return syn.build_grid(cfg, d)
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -212,7 +203,7 @@ def run_ours(args):
         return wave_systems(cfg, systems, wave, k, rank)
 
     opts = dict(rec=rec, precision=32, preco=1, niter=args.niter, tol=1e-8, inner_tol=args.inner_tol,
-                check_every=args.check_every)
+                check_every=args.check_every, max_outer=args.max_outer)
     # pinned host staging for the e2e leg
     pin = {}
 
@@ -309,6 +300,7 @@ def main():
     ap.add_argument("--niter", type=int, default=1000,
                     help="inner iteration budget per system (the reference's niter); lower values are for "
                          "profiling runs, whose systems then stop unconverged")
+    ap.add_argument("--max-outer", type=int, default=30, help="defect-correction cycles per system")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))

@@ -23,7 +23,15 @@ struct csem_ctx {
   DevBuf io[4], sc64, sc32, dotp;
   int nmax64 = 0, nmax32 = 0;
   bool lusgs_pipelined = true;
+  int lusgs_vw = 0;
 };
+
+// the context's kernel-schedule options on one operator set
+template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
+{
+  o.pipelined_sweeps = c->lusgs_pipelined;
+  o.sweep_vw = c->lusgs_vw;
+}
 
 #define API_BEGIN try {
 #define API_END                                                                                          \
@@ -42,7 +50,7 @@ static Ops<F64>* ops64_for(csem_ctx* c, int nsys)
   if (!c->ops64 || c->nmax64 < nsys) {
     delete c->ops64;
     c->ops64 = new Ops<F64>(c->model, nsys, c->st);
-    c->ops64->pipelined_sweeps = c->lusgs_pipelined;
+    configure(c, *c->ops64);
     c->nmax64 = nsys;
   }
   return c->ops64;
@@ -53,7 +61,7 @@ static Ops<F32>* ops32_for(csem_ctx* c, int nsys)
   if (!c->ops32 || c->nmax32 < nsys) {
     delete c->ops32;
     c->ops32 = new Ops<F32>(c->model, nsys, c->st);
-    c->ops32->pipelined_sweeps = c->lusgs_pipelined;
+    configure(c, *c->ops32);
     c->nmax32 = nsys;
   }
   return c->ops32;
@@ -140,16 +148,21 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
 {
   if (!strcmp(name, "lusgs_pipelined")) {
     c->lusgs_pipelined = value != 0;
-    if (c->ops64) c->ops64->pipelined_sweeps = c->lusgs_pipelined;
-    if (c->ops32) c->ops32->pipelined_sweeps = c->lusgs_pipelined;
-    if (c->solver) c->solver->ops.pipelined_sweeps = c->lusgs_pipelined;
-    if (c->batch) {
-      c->batch->o64.pipelined_sweeps = c->lusgs_pipelined;
-      c->batch->o32.pipelined_sweeps = c->lusgs_pipelined;
-    }
-    return CSEM_OK;
+  } else if (!strcmp(name, "lusgs_vw")) {
+    if (value != 0 && value != 1 && value != 2 && value != 4)
+      return csem_set_error(CSEM_EINVAL, "lusgs_vw must be 0, 1, 2 or 4");
+    c->lusgs_vw = value;
+  } else {
+    return csem_set_error(CSEM_EINVAL, "unknown option %s", name);
   }
-  return csem_set_error(CSEM_EINVAL, "unknown option %s", name);
+  if (c->ops64) configure(c, *c->ops64);
+  if (c->ops32) configure(c, *c->ops32);
+  if (c->solver) configure(c, c->solver->ops);
+  if (c->batch) {
+    configure(c, c->batch->o64);
+    configure(c, c->batch->o32);
+  }
+  return CSEM_OK;
 }
 
 int csem_ctx_sync(csem_ctx* c)
@@ -246,7 +259,7 @@ static Solver64* solver_for(csem_ctx* c)
 {
   if (!c->solver) {
     c->solver = new Solver64(c->model, c->st);
-    c->solver->ops.pipelined_sweeps = c->lusgs_pipelined;
+    configure(c, c->solver->ops);
   }
   return c->solver;
 }
@@ -384,8 +397,8 @@ static MixedBatch* batch_for(csem_ctx* c, int nsys)
     delete c->batch;
     c->batch = nullptr;
     c->batch = new MixedBatch(c->model, nsys, c->st);
-    c->batch->o64.pipelined_sweeps = c->lusgs_pipelined;
-    c->batch->o32.pipelined_sweeps = c->lusgs_pipelined;
+    configure(c, c->batch->o64);
+    configure(c, c->batch->o32);
   }
   return c->batch;
 }

@@ -61,7 +61,7 @@ template <class P> struct SweepP {
 
 // one launch per component sweep (pipelined warps, k_lusgs2.cu)
 template <class P>
-void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st);
+void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw);
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK);  // the sweep's rows fit one CTA
 template <class P>
 void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int nslot, cudaStream_t st);

@@ -357,7 +357,7 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
   // dependency of the lexicographic sweep, so they may be mixed sweep by sweep
   auto sweep = [&](int comp, bool fwd) {
     if (pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
-      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st);
+      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st, sweep_vw);
       return;
     }
     const int nd = sweep_diagonals(comp, n1, n2, s.nK);

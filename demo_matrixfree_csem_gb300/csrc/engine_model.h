@@ -84,6 +84,7 @@ class Ops {
   // LU-SGS sweeps: true = one pipelined-warp launch per component sweep (k_lusgs2.cu),
   // false = one launch per wavefront diagonal (k_lusgs.cu); both give identical results
   bool pipelined_sweeps = true;
+  int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
   // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal)
   void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
   void apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);

@@ -31,6 +31,8 @@ namespace csem {
 namespace {
 
 constexpr int MAXROWS = 256;  // rows of one sweep handled by one CTA (a thread each)
+// resident CTAs per SM the register budget is sized for, by points per thread and step
+template <int VW> struct MinBlocks { static constexpr int value = VW >= 4 ? 1 : (VW == 2 ? 2 : 3); };
 
 template <class P> struct View {
   typedef typename P::C C;
@@ -47,10 +49,6 @@ template <class P> struct View {
     return k >= vshift ? Y[c] + idx(c, k - vshift, j, i) : CAP[c] + idx(c, k, j, i);
   }
   __device__ __forceinline__ C ld(int c, int k, int j, int i) const { return *at(c, k, j, i); }
-  __device__ __forceinline__ C ldb(int c, int k, int j, int i) const
-  {
-    return k >= vshift ? X[c][idx(c, k - vshift, j, i)] : P::mk(0, 0);
-  }
 };
 
 template <class P>
@@ -75,17 +73,52 @@ __device__ __forceinline__ View<P> view_of(const SweepP<P>& s, int slot, int sys
   return v;
 }
 
-// (1/a0 + 1/a1)/A + (1/b0 + 1/b1)/B; F64 divides exactly, F32 uses the reciprocals
+// read-only loads (nothing a sweep reads through these is written during the launch)
+template <class T> __device__ __forceinline__ T ro(const T* p) { return __ldg(p); }
+
+// 1-D spacings of one axis at index n: staggered d*s[n], d*s[n-1], cell d*[n] and their
+// reciprocals (the F32 path divides by multiplying)
+template <class P> struct Ax {
+  typename P::R ds, rs, dsm, rsm, d, r;
+};
+// all six values at n >= 1
 template <class P>
-__device__ __forceinline__ typename P::R geo(typename P::R a0, typename P::R ra0, typename P::R a1,
-                                             typename P::R ra1, typename P::R A, typename P::R rA, typename P::R b0,
-                                             typename P::R rb0, typename P::R b1, typename P::R rb1, typename P::R B,
-                                             typename P::R rB)
+__device__ __forceinline__ Ax<P> axis(const typename P::R* d, const typename P::R* ds, const typename P::R* r,
+                                      const typename P::R* rs, int n)
+{
+  Ax<P> a;
+  a.ds = ro(ds + n);
+  a.rs = ro(rs + n);
+  a.dsm = ro(ds + n - 1);
+  a.rsm = ro(rs + n - 1);
+  a.d = ro(d + n);
+  a.r = ro(r + n);
+  return a;
+}
+// the values at n only (n may be 0; dsm/rsm are not used by the caller)
+template <class P>
+__device__ __forceinline__ Ax<P> axis_at(const typename P::R* d, const typename P::R* ds, const typename P::R* r,
+                                         const typename P::R* rs, int n)
+{
+  Ax<P> a;
+  a.ds = ro(ds + n);
+  a.rs = ro(rs + n);
+  a.dsm = 0;
+  a.rsm = 0;
+  a.d = ro(d + n);
+  a.r = ro(r + n);
+  return a;
+}
+
+// (1/a.ds + 1/a.dsm)/a.d + (1/b.ds + 1/b.dsm)/b.d; F64 divides exactly, F32 multiplies
+// by the reciprocals
+template <class P>
+__device__ __forceinline__ typename P::R geo(const Ax<P>& a, const Ax<P>& b)
 {
   typedef typename P::R R;
   const R one = 1;
-  return P::add(P::divs(P::add(P::divs(one, a0, ra0), P::divs(one, a1, ra1)), A, rA),
-                P::divs(P::add(P::divs(one, b0, rb0), P::divs(one, b1, rb1)), B, rB));
+  return P::add(P::divs(P::add(P::divs(one, a.ds, a.rs), P::divs(one, a.dsm, a.rsm)), a.d, a.r),
+                P::divs(P::add(P::divs(one, b.ds, b.rs), P::divs(one, b.dsm, b.rsm)), b.d, b.r));
 }
 
 // (b - aij) / aii: Smith's quotient in F64, a * conj(d) / |d|^2 in F32
@@ -115,78 +148,70 @@ __device__ __forceinline__ typename P::C fin(typename P::C b, typename P::C aij,
 }
 
 // --- per-point updates in the reference's operation order; the component being
-// updated is zero at its own point while its row is evaluated (fdfd.c:357,383,409)
+// updated is zero at its own point while its row is evaluated (fdfd.c:357,383,409).
+// X, Y, Z are the spacings at the point's i, j, k.
 
 // Ex at (k,j,i): fdfd.c:358-369
 template <class P>
-__device__ __forceinline__ typename P::C upd_ex(const GridP<P>& g, const SysScal<P>& sc, int k, int j, int i,
-                                                typename P::C eyA, typename P::C eyB, typename P::C eyC,
-                                                typename P::C eyD, typename P::C exjp, typename P::C exjm,
-                                                typename P::C exkp, typename P::C exkm, typename P::C ezA,
-                                                typename P::C ezB, typename P::C ezC, typename P::C ezD,
-                                                typename P::C b, typename P::R sg)
+__device__ __forceinline__ typename P::C upd_ex(const SysScal<P>& sc, int fvm, const Ax<P>& X, const Ax<P>& Y,
+                                                const Ax<P>& Z, typename P::C eyA, typename P::C eyB,
+                                                typename P::C eyC, typename P::C eyD, typename P::C exjp,
+                                                typename P::C exjm, typename P::C exkp, typename P::C exkm,
+                                                typename P::C ezA, typename P::C ezB, typename P::C ezC,
+                                                typename P::C ezD, typename P::C b, typename P::R sg)
 {
   typedef typename P::C C;
   const C own = czero<P>();
-  C t1 = csub<P>(cdivs<P>(csub<P>(eyA, eyB), g.d1s[i], g.r1s[i]), cdivs<P>(csub<P>(exjp, own), g.d2s[j], g.r2s[j]));
-  C t2 = csub<P>(cdivs<P>(csub<P>(eyC, eyD), g.d1s[i], g.r1s[i]), cdivs<P>(csub<P>(own, exjm), g.d2s[j - 1], g.r2s[j - 1]));
-  C t3 = csub<P>(cdivs<P>(csub<P>(exkp, own), g.d3s[k], g.r3s[k]), cdivs<P>(csub<P>(ezA, ezB), g.d1s[i], g.r1s[i]));
-  C t4 = csub<P>(cdivs<P>(csub<P>(own, exkm), g.d3s[k - 1], g.r3s[k - 1]), cdivs<P>(csub<P>(ezC, ezD), g.d1s[i], g.r1s[i]));
-  C aij = csub<P>(cmul<P>(csub<P>(cdivs<P>(csub<P>(t1, t2), g.d2[j], g.r2[j]), cdivs<P>(csub<P>(t3, t4), g.d3[k], g.r3[k])),
-                          sc.iwmu),
+  C t1 = csub<P>(cdivs<P>(csub<P>(eyA, eyB), X.ds, X.rs), cdivs<P>(csub<P>(exjp, own), Y.ds, Y.rs));
+  C t2 = csub<P>(cdivs<P>(csub<P>(eyC, eyD), X.ds, X.rs), cdivs<P>(csub<P>(own, exjm), Y.dsm, Y.rsm));
+  C t3 = csub<P>(cdivs<P>(csub<P>(exkp, own), Z.ds, Z.rs), cdivs<P>(csub<P>(ezA, ezB), X.ds, X.rs));
+  C t4 = csub<P>(cdivs<P>(csub<P>(own, exkm), Z.dsm, Z.rsm), cdivs<P>(csub<P>(ezC, ezD), X.ds, X.rs));
+  C aij = csub<P>(cmul<P>(csub<P>(cdivs<P>(csub<P>(t1, t2), Y.d, Y.r), cdivs<P>(csub<P>(t3, t4), Z.d, Z.r)), sc.iwmu),
                   rmul<P>(sg, own));
-  typename P::R gg = geo<P>(g.d2s[j], g.r2s[j], g.d2s[j - 1], g.r2s[j - 1], g.d2[j], g.r2[j], g.d3s[k], g.r3s[k],
-                            g.d3s[k - 1], g.r3s[k - 1], g.d3[k], g.r3[k]);
-  typename P::R vol = g.fvm ? P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[k]) : 0;
-  return fin<P>(b, aij, gg, sg, vol, sc, g.fvm);
+  typename P::R vol = fvm ? P::mul(P::mul(X.ds, Y.d), Z.d) : 0;
+  return fin<P>(b, aij, geo<P>(Y, Z), sg, vol, sc, fvm);
 }
 
 // Ey at (k,j,i): fdfd.c:384-395
 template <class P>
-__device__ __forceinline__ typename P::C upd_ey(const GridP<P>& g, const SysScal<P>& sc, int k, int j, int i,
-                                                typename P::C ezA, typename P::C ezB, typename P::C ezC,
-                                                typename P::C ezD, typename P::C eykp, typename P::C eykm,
-                                                typename P::C eyip, typename P::C eyim, typename P::C exA,
-                                                typename P::C exB, typename P::C exC, typename P::C exD,
-                                                typename P::C b, typename P::R sg)
+__device__ __forceinline__ typename P::C upd_ey(const SysScal<P>& sc, int fvm, const Ax<P>& X, const Ax<P>& Y,
+                                                const Ax<P>& Z, typename P::C ezA, typename P::C ezB,
+                                                typename P::C ezC, typename P::C ezD, typename P::C eykp,
+                                                typename P::C eykm, typename P::C eyip, typename P::C eyim,
+                                                typename P::C exA, typename P::C exB, typename P::C exC,
+                                                typename P::C exD, typename P::C b, typename P::R sg)
 {
   typedef typename P::C C;
   const C own = czero<P>();
-  C t1 = csub<P>(cdivs<P>(csub<P>(ezA, ezB), g.d2s[j], g.r2s[j]), cdivs<P>(csub<P>(eykp, own), g.d3s[k], g.r3s[k]));
-  C t2 = csub<P>(cdivs<P>(csub<P>(ezC, ezD), g.d2s[j], g.r2s[j]), cdivs<P>(csub<P>(own, eykm), g.d3s[k - 1], g.r3s[k - 1]));
-  C t3 = csub<P>(cdivs<P>(csub<P>(eyip, own), g.d1s[i], g.r1s[i]), cdivs<P>(csub<P>(exA, exB), g.d2s[j], g.r2s[j]));
-  C t4 = csub<P>(cdivs<P>(csub<P>(own, eyim), g.d1s[i - 1], g.r1s[i - 1]), cdivs<P>(csub<P>(exC, exD), g.d2s[j], g.r2s[j]));
-  C aij = csub<P>(cmul<P>(csub<P>(cdivs<P>(csub<P>(t1, t2), g.d3[k], g.r3[k]), cdivs<P>(csub<P>(t3, t4), g.d1[i], g.r1[i])),
-                          sc.iwmu),
+  C t1 = csub<P>(cdivs<P>(csub<P>(ezA, ezB), Y.ds, Y.rs), cdivs<P>(csub<P>(eykp, own), Z.ds, Z.rs));
+  C t2 = csub<P>(cdivs<P>(csub<P>(ezC, ezD), Y.ds, Y.rs), cdivs<P>(csub<P>(own, eykm), Z.dsm, Z.rsm));
+  C t3 = csub<P>(cdivs<P>(csub<P>(eyip, own), X.ds, X.rs), cdivs<P>(csub<P>(exA, exB), Y.ds, Y.rs));
+  C t4 = csub<P>(cdivs<P>(csub<P>(own, eyim), X.dsm, X.rsm), cdivs<P>(csub<P>(exC, exD), Y.ds, Y.rs));
+  C aij = csub<P>(cmul<P>(csub<P>(cdivs<P>(csub<P>(t1, t2), Z.d, Z.r), cdivs<P>(csub<P>(t3, t4), X.d, X.r)), sc.iwmu),
                   rmul<P>(sg, own));
-  typename P::R gg = geo<P>(g.d3s[k], g.r3s[k], g.d3s[k - 1], g.r3s[k - 1], g.d3[k], g.r3[k], g.d1s[i], g.r1s[i],
-                            g.d1s[i - 1], g.r1s[i - 1], g.d1[i], g.r1[i]);
-  typename P::R vol = g.fvm ? P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[k]) : 0;  // Ex's volume (fdfd.c:391)
-  return fin<P>(b, aij, gg, sg, vol, sc, g.fvm);
+  typename P::R vol = fvm ? P::mul(P::mul(X.ds, Y.d), Z.d) : 0;  // Ex's volume (fdfd.c:391)
+  return fin<P>(b, aij, geo<P>(Z, X), sg, vol, sc, fvm);
 }
 
 // Ez at (k,j,i): fdfd.c:410-421
 template <class P>
-__device__ __forceinline__ typename P::C upd_ez(const GridP<P>& g, const SysScal<P>& sc, int k, int j, int i,
-                                                typename P::C exA, typename P::C exB, typename P::C exC,
-                                                typename P::C exD, typename P::C ezip, typename P::C ezim,
-                                                typename P::C ezjp, typename P::C ezjm, typename P::C eyA,
-                                                typename P::C eyB, typename P::C eyC, typename P::C eyD,
-                                                typename P::C b, typename P::R sg)
+__device__ __forceinline__ typename P::C upd_ez(const SysScal<P>& sc, int fvm, const Ax<P>& X, const Ax<P>& Y,
+                                                const Ax<P>& Z, typename P::C exA, typename P::C exB,
+                                                typename P::C exC, typename P::C exD, typename P::C ezip,
+                                                typename P::C ezim, typename P::C ezjp, typename P::C ezjm,
+                                                typename P::C eyA, typename P::C eyB, typename P::C eyC,
+                                                typename P::C eyD, typename P::C b, typename P::R sg)
 {
   typedef typename P::C C;
   const C own = czero<P>();
-  C t1 = csub<P>(cdivs<P>(csub<P>(exA, exB), g.d3s[k], g.r3s[k]), cdivs<P>(csub<P>(ezip, own), g.d1s[i], g.r1s[i]));
-  C t2 = csub<P>(cdivs<P>(csub<P>(exC, exD), g.d3s[k], g.r3s[k]), cdivs<P>(csub<P>(own, ezim), g.d1s[i - 1], g.r1s[i - 1]));
-  C t3 = csub<P>(cdivs<P>(csub<P>(ezjp, own), g.d2s[j], g.r2s[j]), cdivs<P>(csub<P>(eyA, eyB), g.d3s[k], g.r3s[k]));
-  C t4 = csub<P>(cdivs<P>(csub<P>(own, ezjm), g.d2s[j - 1], g.r2s[j - 1]), cdivs<P>(csub<P>(eyC, eyD), g.d3s[k], g.r3s[k]));
-  C aij = csub<P>(cmul<P>(csub<P>(cdivs<P>(csub<P>(t1, t2), g.d1[i], g.r1[i]), cdivs<P>(csub<P>(t3, t4), g.d2[j], g.r2[j])),
-                          sc.iwmu),
+  C t1 = csub<P>(cdivs<P>(csub<P>(exA, exB), Z.ds, Z.rs), cdivs<P>(csub<P>(ezip, own), X.ds, X.rs));
+  C t2 = csub<P>(cdivs<P>(csub<P>(exC, exD), Z.ds, Z.rs), cdivs<P>(csub<P>(own, ezim), X.dsm, X.rsm));
+  C t3 = csub<P>(cdivs<P>(csub<P>(ezjp, own), Y.ds, Y.rs), cdivs<P>(csub<P>(eyA, eyB), Z.ds, Z.rs));
+  C t4 = csub<P>(cdivs<P>(csub<P>(own, ezjm), Y.dsm, Y.rsm), cdivs<P>(csub<P>(eyC, eyD), Z.ds, Z.rs));
+  C aij = csub<P>(cmul<P>(csub<P>(cdivs<P>(csub<P>(t1, t2), X.d, X.r), cdivs<P>(csub<P>(t3, t4), Y.d, Y.r)), sc.iwmu),
                   rmul<P>(sg, own));
-  typename P::R gg = geo<P>(g.d1s[i], g.r1s[i], g.d1s[i - 1], g.r1s[i - 1], g.d1[i], g.r1[i], g.d2s[j], g.r2s[j],
-                            g.d2s[j - 1], g.r2s[j - 1], g.d2[j], g.r2[j]);
-  typename P::R vol = g.fvm ? P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[k]) : 0;  // Ex's volume (fdfd.c:417)
-  return fin<P>(b, aij, gg, sg, vol, sc, g.fvm);
+  typename P::R vol = fvm ? P::mul(P::mul(X.ds, Y.d), Z.d) : 0;  // Ex's volume (fdfd.c:417)
+  return fin<P>(b, aij, geo<P>(X, Y), sg, vol, sc, fvm);
 }
 
 template <class C> __device__ __forceinline__ C shfl_up(C v)
@@ -232,7 +257,7 @@ __device__ __forceinline__ void hand_over(const C (&res)[VW], C (*hand)[2][VW], 
 
 // Ex sweep: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
 template <class P, bool FWD, int VW>
-__global__ void __launch_bounds__(MAXROWS) k_sweep_ex(SweepP<P> s)
+__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
@@ -240,15 +265,21 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_ex(SweepP<P> s)
   const int slot = blockIdx.y;
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
-  const int n1 = g.n1, nK = s.nK;
+  const int n1 = g.n1, n2 = g.n2, nK = s.nK;
   const int i0 = blockIdx.x * VW;
   const View<P> V = view_of<P>(s, slot, sys);
   const SysScal<P> sc = s.scal[sys];
   const C z = czero<P>();
-  const int R_ = nK - 1, M = g.n2 - 1;  // rows k = 1..R_, march j = 1..M
+  const int R_ = nK - 1, M = n2 - 1;  // rows k = 1..R_, march j = 1..M
   const int rr = threadIdx.x;
   const bool rowok = rr < R_;
   const int k = FWD ? 1 + rr : R_ - rr;
+  // spacings fixed for this thread: k (row) and the VW i's
+  const Ax<P> Z = rowok ? axis<P>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<P>{};
+  Ax<P> X[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++)
+    X[q] = i0 + q < n1 ? axis_at<P>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<P>{};
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
@@ -258,25 +289,26 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_ex(SweepP<P> s)
     const int c = T - rr;
     if (rowok && c >= 0 && c < M) {
       const int j = FWD ? 1 + c : M - c;
+      const Ax<P> Y = axis<P>(g.d2, g.d2s, g.r2, g.r2s, j);
       C exjm[VW], exkm[VW], b[VW], eyA[VW], eyB[VW], eyC[VW], eyD[VW], ezA[VW], ezB[VW], ezC[VW], ezD[VW];
       R sg[VW];
 #pragma unroll
       for (int q = 0; q < VW; q++) {  // loads: nothing read here is written in this step
         const int i = i0 + q;
         if (i < n1) {
-          b[q] = V.ldb(0, k, j, i);
-          sg[q] = g.s11[ix1(g.n1, g.n2, k, j, i)];
+          b[q] = k >= V.vshift ? ro(V.X[0] + V.idx(0, k - V.vshift, j, i)) : z;
+          sg[q] = ro(g.s11 + ix1(n1, n2, k, j, i));
           if (!FWD) {
             exjm[q] = V.ld(0, k, j - 1, i);
             exkm[q] = V.ld(0, k - 1, j, i);
-            eyA[q] = V.ld(1, k, j, i + 1);
-            eyB[q] = V.ld(1, k, j, i);
-            eyC[q] = V.ld(1, k, j - 1, i + 1);
-            eyD[q] = V.ld(1, k, j - 1, i);
-            ezA[q] = V.ld(2, k, j, i + 1);
-            ezB[q] = V.ld(2, k, j, i);
-            ezC[q] = V.ld(2, k - 1, j, i + 1);
-            ezD[q] = V.ld(2, k - 1, j, i);
+            eyA[q] = ro(V.at(1, k, j, i + 1));
+            eyB[q] = ro(V.at(1, k, j, i));
+            eyC[q] = ro(V.at(1, k, j - 1, i + 1));
+            eyD[q] = ro(V.at(1, k, j - 1, i));
+            ezA[q] = ro(V.at(2, k, j, i + 1));
+            ezB[q] = ro(V.at(2, k, j, i));
+            ezC[q] = ro(V.at(2, k - 1, j, i + 1));
+            ezD[q] = ro(V.at(2, k - 1, j, i));
           }
         }
       }
@@ -289,10 +321,10 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_ex(SweepP<P> s)
         }
         C v;
         if (FWD)  // own row: j-1 is the previous step's value; row k-1 is the neighbour
-          v = upd_ex<P>(g, sc, k, j, i, z, z, z, z, z, res[q], z, nb[q], z, z, z, z, b[q], sg[q]);
+          v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, z, z, z, z, z, res[q], z, nb[q], z, z, z, z, b[q], sg[q]);
         else      // own row: j+1 is the previous step's value; row k+1 is the neighbour
-          v = upd_ex<P>(g, sc, k, j, i, eyA[q], eyB[q], eyC[q], eyD[q], res[q], exjm[q], nb[q], exkm[q], ezA[q],
-                        ezB[q], ezC[q], ezD[q], b[q], sg[q]);
+          v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, eyA[q], eyB[q], eyC[q], eyD[q], res[q], exjm[q], nb[q], exkm[q],
+                        ezA[q], ezB[q], ezC[q], ezD[q], b[q], sg[q]);
         *V.at(0, k, j, i) = v;
         res[q] = v;
       }
@@ -307,7 +339,7 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_ex(SweepP<P> s)
 // Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j) sweeps, march i in chunks
 // of VW. grid (lines, systems)
 template <class P, int COMP, bool FWD, int VW>
-__global__ void __launch_bounds__(MAXROWS) k_sweep_eyz(SweepP<P> s)
+__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
@@ -328,6 +360,15 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_eyz(SweepP<P> s)
   const int r = FWD ? 1 + rr : R_ - rr;
   const int k = COMP == 1 ? r : line;
   const int j = COMP == 1 ? line : r;
+  // spacings fixed for this thread: the line's and the row's
+  Ax<P> Y, Z;
+  if (COMP == 1) {
+    Y = axis_at<P>(g.d2, g.d2s, g.r2, g.r2s, j);
+    Z = rowok ? axis<P>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<P>{};
+  } else {
+    Y = rowok ? axis<P>(g.d2, g.d2s, g.r2, g.r2s, j) : Ax<P>{};
+    Z = axis_at<P>(g.d3, g.d3s, g.r3, g.r3s, k);
+  }
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
@@ -337,51 +378,45 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_eyz(SweepP<P> s)
     const int c = T - rr;
     if (rowok && c >= 0 && c < NC) {
       C prev = c > 0 ? res[VW - 1] : z;  // own row at the previous march position
-      C b[VW], xA[VW], xB[VW], xC[VW], xD[VW], yA[VW], yB[VW], yC[VW], yD[VW], own2[VW];
+      C b[VW], xA[VW], xB[VW], xC[VW], xD[VW], yA[VW], yB[VW], yC[VW], yD[VW], own2[VW], rowold[VW];
       R sg[VW];
+      Ax<P> X[VW];
 #pragma unroll
-      for (int q = 0; q < VW; q++) {  // loads
+      for (int q = 0; q < VW; q++) {  // loads: nothing read here is written in this step
         const int m = c * VW + q;
         if (m < M) {
           const int i = FWD ? 1 + m : M - m;
+          X[q] = axis<P>(g.d1, g.d1s, g.r1, g.r1s, i);
+          const int cc = COMP;
+          b[q] = k >= V.vshift ? ro(V.X[cc] + V.idx(cc, k - V.vshift, j, i)) : z;
           if (COMP == 1) {
-            b[q] = V.ldb(1, k, j, i);
-            sg[q] = g.s22[ix2(g.n1, g.n2, k, j, i)];
-            xA[q] = V.ld(0, k, j + 1, i);
-            xB[q] = V.ld(0, k, j, i);
-            xC[q] = V.ld(0, k, j + 1, i - 1);
-            xD[q] = V.ld(0, k, j, i - 1);
-            if (!FWD) {
-              yA[q] = V.ld(2, k, j + 1, i);
-              yB[q] = V.ld(2, k, j, i);
-              yC[q] = V.ld(2, k - 1, j + 1, i);
-              yD[q] = V.ld(2, k - 1, j, i);
-              own2[q] = V.ld(1, k, j, i - 1);  // Ey(i-1): not yet swept backward
-              // Ey(k-1): the next row's old value
+            sg[q] = ro(g.s22 + ix2(n1, n2, k, j, i));
+            xA[q] = ro(V.at(0, k, j + 1, i));
+            xB[q] = ro(V.at(0, k, j, i));
+            xC[q] = ro(V.at(0, k, j + 1, i - 1));
+            xD[q] = ro(V.at(0, k, j, i - 1));
+            if (!FWD) {  // Ez, this row's next position, and the next row's old value
+              yA[q] = ro(V.at(2, k, j + 1, i));
+              yB[q] = ro(V.at(2, k, j, i));
+              yC[q] = ro(V.at(2, k - 1, j + 1, i));
+              yD[q] = ro(V.at(2, k - 1, j, i));
+              own2[q] = V.ld(1, k, j, i - 1);
+              rowold[q] = V.ld(1, k - 1, j, i);
             }
           } else {
-            b[q] = V.ldb(2, k, j, i);
-            sg[q] = g.s33[ix3(g.n1, g.n2, k, j, i)];
-            xA[q] = V.ld(0, k + 1, j, i);
-            xB[q] = V.ld(0, k, j, i);
-            xC[q] = V.ld(0, k + 1, j, i - 1);
-            xD[q] = V.ld(0, k, j, i - 1);
-            yA[q] = V.ld(1, k + 1, j, i);
-            yB[q] = V.ld(1, k, j, i);
-            yC[q] = V.ld(1, k + 1, j - 1, i);
-            yD[q] = V.ld(1, k, j - 1, i);
-            if (!FWD) own2[q] = V.ld(2, k, j, i - 1);  // Ez(i-1): not yet swept backward
-          }
-        }
-      }
-      C rowold[VW];  // backward: the next row's forward value at this position
-      if (!FWD) {
-#pragma unroll
-        for (int q = 0; q < VW; q++) {
-          const int m = c * VW + q;
-          if (m < M) {
-            const int i = M - m;
-            rowold[q] = COMP == 1 ? V.ld(1, k - 1, j, i) : V.ld(2, k, j - 1, i);
+            sg[q] = ro(g.s33 + ix3(n1, n2, k, j, i));
+            xA[q] = ro(V.at(0, k + 1, j, i));
+            xB[q] = ro(V.at(0, k, j, i));
+            xC[q] = ro(V.at(0, k + 1, j, i - 1));
+            xD[q] = ro(V.at(0, k, j, i - 1));
+            yA[q] = ro(V.at(1, k + 1, j, i));
+            yB[q] = ro(V.at(1, k, j, i));
+            yC[q] = ro(V.at(1, k + 1, j - 1, i));
+            yD[q] = ro(V.at(1, k, j - 1, i));
+            if (!FWD) {
+              own2[q] = V.ld(2, k, j, i - 1);
+              rowold[q] = V.ld(2, k, j - 1, i);
+            }
           }
         }
       }
@@ -396,18 +431,19 @@ __global__ void __launch_bounds__(MAXROWS) k_sweep_eyz(SweepP<P> s)
         C v;
         if (COMP == 1) {
           if (FWD)
-            v = upd_ey<P>(g, sc, k, j, i, z, z, z, z, z, nb[q], z, prev, xA[q], xB[q], xC[q], xD[q], b[q], sg[q]);
+            v = upd_ey<P>(sc, g.fvm, X[q], Y, Z, z, z, z, z, z, nb[q], z, prev, xA[q], xB[q], xC[q], xD[q], b[q],
+                          sg[q]);
           else
-            v = upd_ey<P>(g, sc, k, j, i, yA[q], yB[q], yC[q], yD[q], nb[q], rowold[q], prev, own2[q], xA[q], xB[q],
-                          xC[q], xD[q], b[q], sg[q]);
+            v = upd_ey<P>(sc, g.fvm, X[q], Y, Z, yA[q], yB[q], yC[q], yD[q], nb[q], rowold[q], prev, own2[q], xA[q],
+                          xB[q], xC[q], xD[q], b[q], sg[q]);
           *V.at(1, k, j, i) = v;
         } else {
           if (FWD)
-            v = upd_ez<P>(g, sc, k, j, i, xA[q], xB[q], xC[q], xD[q], z, prev, z, nb[q], yA[q], yB[q], yC[q], yD[q],
-                          b[q], sg[q]);
+            v = upd_ez<P>(sc, g.fvm, X[q], Y, Z, xA[q], xB[q], xC[q], xD[q], z, prev, z, nb[q], yA[q], yB[q], yC[q],
+                          yD[q], b[q], sg[q]);
           else
-            v = upd_ez<P>(g, sc, k, j, i, xA[q], xB[q], xC[q], xD[q], prev, own2[q], nb[q], rowold[q], yA[q], yB[q],
-                          yC[q], yD[q], b[q], sg[q]);
+            v = upd_ez<P>(sc, g.fvm, X[q], Y, Z, xA[q], xB[q], xC[q], xD[q], prev, own2[q], nb[q], rowold[q], yA[q],
+                          yB[q], yC[q], yD[q], b[q], sg[q]);
           *V.at(2, k, j, i) = v;
         }
         res[q] = v;
@@ -427,11 +463,9 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
   return rows >= 1 && rows <= MAXROWS && n1 >= 2 && n2 >= 2;
 }
 
-template <class P>
-void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st)
+template <class P, int VW>
+static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st)
 {
-  // points per thread and step: 4 complex64 (one 32-byte sector), 2 complex128
-  constexpr int VW = P::exact ? 2 : 4;
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
   const int threads = (rows + 31) / 32 * 32;
@@ -450,7 +484,18 @@ void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, c
   }
 }
 
-template void launch_sweep_pipelined<F64>(const SweepP<F64>&, int, bool, int, cudaStream_t);
-template void launch_sweep_pipelined<F32>(const SweepP<F32>&, int, bool, int, cudaStream_t);
+// vw: points per thread and step (1, 2 or 4; other values select the default, the
+// fastest measured on a 200x140x140 grid: 2 for complex64, 1 for complex128)
+template <class P>
+void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw)
+{
+  if (vw != 1 && vw != 2 && vw != 4) vw = P::exact ? 1 : 2;
+  if (vw == 1) launch_vw<P, 1>(s, comp, fwd, nslot, st);
+  else if (vw == 2) launch_vw<P, 2>(s, comp, fwd, nslot, st);
+  else launch_vw<P, 4>(s, comp, fwd, nslot, st);
+}
+
+template void launch_sweep_pipelined<F64>(const SweepP<F64>&, int, bool, int, cudaStream_t, int);
+template void launch_sweep_pipelined<F32>(const SweepP<F32>&, int, bool, int, cudaStream_t, int);
 
 }  // namespace csem

@@ -1,0 +1,86 @@
+"""Operator micro-benchmark: time A, LU-SGS or A-phi applications on a batch of systems.
+
+    python -m demo_matrixfree_csem_gb300.opbench --workload marlim_like_96 --op lusgs \
+        --prec 32 --nsys 16 --reps 5 [--schedule pipelined|diagonal] [--vw 0|1|2|4]
+
+Vectors are random and stay on the device; each repetition applies the operator to all
+systems once through the device-pointer C ABI (csem_*_apply_dev) on the context's
+stream, timed with CUDA events on that stream. Prints one JSON line: milliseconds per
+application and per system, and the algorithmic HBM rate (bytes per system per
+application: A 40/20 B per unknown, LU-SGS 96/48 B per unknown of the LU-SGS grid, in
+complex128/complex64). With --reps 1 --warmup 0 it is a small, fixed launch sequence for
+profilers.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import tempfile
+
+import numpy as np
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--workload", default="marlim_like_96")
+    ap.add_argument("--op", choices=["A", "lusgs", "aphi"], default="lusgs")
+    ap.add_argument("--prec", type=int, choices=[32, 64], default=32)
+    ap.add_argument("--nsys", type=int, default=16)
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--freq", type=float, default=0.5)
+    ap.add_argument("--schedule", choices=["pipelined", "diagonal"], default="pipelined")
+    ap.add_argument("--vw", type=int, default=0)
+    a = ap.parse_args(argv)
+
+    import torch
+    from . import api, synthetic
+    cfg = synthetic.workload(a.workload)
+    airbc = int(cfg.params.get("airbc", 0))
+    with tempfile.TemporaryDirectory() as d:
+        G = synthetic.build_grid(cfg, d)
+    ctx = api.Ctx(G, airbc, 0)
+    ctx.set_option("lusgs_pipelined", 1 if a.schedule == "pipelined" else 0)
+    ctx.set_option("lusgs_vw", a.vw)
+    dt = torch.complex64 if a.prec == 32 else torch.complex128
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    x = torch.randn(a.nsys, ctx.lE, dtype=dt, device="cuda", generator=gen)
+    y = torch.empty_like(x)
+    iom = np.zeros(2 * a.nsys)
+    iom[1::2] = api.iom_of(a.freq).imag
+    fn = {"A": api.lib().csem_fdfd_apply_dev, "lusgs": api.lib().csem_lusgs_apply_dev,
+          "aphi": api.lib().csem_aphi_apply_dev}[a.op]
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def apply():
+        rc = fn(ctx.h, a.prec, a.nsys, iom.ctypes.data_as(C.POINTER(C.c_double)), C.c_void_p(x.data_ptr()),
+                C.c_void_p(y.data_ptr()), None)
+        if rc:
+            raise api.CsemError(rc, api.lib().csem_last_error().decode())
+
+    for _ in range(a.warmup):
+        apply()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.reps):
+        apply()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / a.reps
+    nf = (ctx.n1 * (ctx.n2 + 1) * (ctx.n3f + 1) + (ctx.n1 + 1) * ctx.n2 * (ctx.n3f + 1)
+          + (ctx.n1 + 1) * (ctx.n2 + 1) * ctx.n3f)
+    bc = 16 if a.prec == 64 else 8
+    bs = bc // 2
+    per_sys = {"A": (2 * bc + bs) * ctx.lE, "lusgs": (5 * bc + 2 * bs) * nf, "aphi": None}[a.op]
+    out = {"workload": a.workload, "op": a.op, "prec": a.prec, "nsys": a.nsys, "schedule": a.schedule,
+           "vw": a.vw, "ms_per_application": ms, "ms_per_system": ms / a.nsys,
+           "algorithmic_bytes_per_system": per_sys,
+           "algorithmic_GBps": per_sys * a.nsys / (ms * 1e-3) / 1e9 if per_sys else None}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

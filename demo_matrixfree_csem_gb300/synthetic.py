@@ -223,3 +223,27 @@ def random_small(seed: int, nx=12, ny=10, nz=9, airbc=0, nb=3, aniso=True, stret
                   lextend="3000")
     params.update(extra)
     return Config(model, Acquisition(src, rec), params, name=model.name)
+
+
+WORKLOADS = {"marlim_like_96": lambda: marlim_like(seed=0), "layered_120": layered_120,
+             "vti_block_120": vti_block_120}
+
+
+def workload(name: str) -> Config:
+    """A named benchmark workload (marlim_like_96, layered_120, vti_block_120)."""
+    if name not in WORKLOADS:
+        raise ValueError(f"unknown workload {name}; known: {', '.join(WORKLOADS)}")
+    return WORKLOADS[name]()
+
+
+def build_grid(cfg: Config, d: str):
+    """Write `cfg` into directory d and run the product's host set-up on it (read,
+    extend with the config's nb/lextend, airwave tables when airbc=1)."""
+    from .api import Grid
+    write_config(cfg, d)
+    p = cfg.params
+    G = Grid.from_files(*[os.path.join(d, n) for n in ("fx1", "fx2", "fx3", "frho11", "frho22", "frho33")])
+    G.extend(int(p.get("nb", 15)), float(p.get("lextend", -1)), float(p.get("rho_air", 1e6)), int(p.get("istretch", 1)))
+    if int(p.get("airbc", 0)):
+        G.airbc(int(p.get("n1fft", 1024)), int(p.get("n2fft", 1024)))
+    return G

@@ -154,9 +154,12 @@ int csem_cdot_dev_noalloc(int prec, long n, int nsys, const void *a, const void 
 int csem_ctx_sync(csem_ctx *c);
 /* the context's CUDA stream (a cudaStream_t), for callers that record events on it */
 void *csem_ctx_stream(csem_ctx *c);
-/* Kernel-schedule options (results do not depend on them):
- *   "lusgs_pipelined" 1 (default): one pipelined-warp launch per LU-SGS component sweep;
- *                     0: one launch per wavefront diagonal. */
+/* Kernel-schedule options. complex128 results do not depend on them; complex64 results
+ * may differ in the last bits between schedules:
+ *   "lusgs_pipelined" 1 (default): one launch per LU-SGS component sweep, rows as a
+ *                     lockstep pipeline; 0: one launch per wavefront diagonal;
+ *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
+ *                     0 for the default (2 complex64, 1 complex128). */
 int csem_ctx_set_option(csem_ctx *c, const char *name, int value);
 
 /* ------------------------------------------------------------ timing

@@ -120,14 +120,15 @@ def test_larger_grid_bit_exact(gpu, tmp_path, airbc, fvm):
     else:
         assert np.array_equal(ya, yo)
     mo = O.lusgs(x)
-    for sched in (1, 0):  # pipelined warps and one launch per diagonal: same order, same bits
+    # lockstep row pipelines (any points-per-thread width) and one launch per diagonal
+    # visit the points in dependency order with the same arithmetic: same bits
+    for sched, vw in ((1, 0), (1, 1), (1, 2), (1, 4), (0, 0)):
         ctx.set_option("lusgs_pipelined", sched)
-        assert np.array_equal(ctx.lusgs_apply(iom, x), mo), sched
-    ctx.set_option("lusgs_pipelined", 0)
-    m32_diag = ctx.lusgs_apply(iom, x, c64=True)
+        ctx.set_option("lusgs_vw", vw)
+        assert np.array_equal(ctx.lusgs_apply(iom, x), mo), (sched, vw)
+        assert relerr(ctx.lusgs_apply(iom, x, c64=True), mo) <= 2e-5, (sched, vw)
     ctx.set_option("lusgs_pipelined", 1)
-    m32_pipe = ctx.lusgs_apply(iom, x, c64=True)
-    assert relerr(m32_pipe, mo) <= 2e-5 and relerr(m32_diag, mo) <= 2e-5
+    ctx.set_option("lusgs_vw", 0)
 
 
 @pytest.mark.parametrize("airbc", [0, 1])
