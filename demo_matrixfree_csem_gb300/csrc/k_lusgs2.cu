@@ -49,6 +49,14 @@ template <class P> struct View {
     return k >= vshift ? Y[c] + idx(c, k - vshift, j, i) : CAP[c] + idx(c, k, j, i);
   }
   __device__ __forceinline__ C ld(int c, int k, int j, int i) const { return *at(c, k, j, i); }
+  // start of row (k, j) of component c (element i of the row is row[i]); rows of one
+  // plane are row_len(c) elements apart
+  __device__ __forceinline__ C* row(int c, int k, int j) const { return at(c, k, j, 0); }
+  __device__ __forceinline__ const C* brow(int c, int k, int j) const
+  {
+    return k >= vshift ? X[c] + idx(c, k - vshift, j, 0) : nullptr;
+  }
+  __device__ __forceinline__ int row_len(int c) const { return c == 0 ? n1 : n1 + 1; }
 };
 
 template <class P>
@@ -280,6 +288,21 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
 #pragma unroll
   for (int q = 0; q < VW; q++)
     X[q] = i0 + q < n1 ? axis_at<P>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<P>{};
+  // planes this thread reads and writes, offset to its first i; row j is j * row_len
+  C* ex0 = nullptr;
+  const C *ex1 = nullptr, *ey0 = nullptr, *ez0 = nullptr, *ez1 = nullptr, *bb = nullptr;
+  const R* sg0 = nullptr;
+  if (rowok) {
+    ex0 = V.row(0, k, 0) + i0;
+    ex1 = V.row(0, k - 1, 0) + i0;
+    ey0 = V.row(1, k, 0) + i0;
+    ez0 = V.row(2, k, 0) + i0;
+    ez1 = V.row(2, k - 1, 0) + i0;
+    bb = V.brow(0, k, 0);
+    if (bb) bb += i0;
+    sg0 = g.s11 + ix1(n1, n2, k, 0, i0);
+  }
+  const int L1 = n1 + 1;
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
@@ -290,32 +313,31 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
     if (rowok && c >= 0 && c < M) {
       const int j = FWD ? 1 + c : M - c;
       const Ax<P> Y = axis<P>(g.d2, g.d2s, g.r2, g.r2s, j);
+      const int ox = j * n1, oy = j * L1;
       C exjm[VW], exkm[VW], b[VW], eyA[VW], eyB[VW], eyC[VW], eyD[VW], ezA[VW], ezB[VW], ezC[VW], ezD[VW];
       R sg[VW];
 #pragma unroll
       for (int q = 0; q < VW; q++) {  // loads: nothing read here is written in this step
-        const int i = i0 + q;
-        if (i < n1) {
-          b[q] = k >= V.vshift ? ro(V.X[0] + V.idx(0, k - V.vshift, j, i)) : z;
-          sg[q] = ro(g.s11 + ix1(n1, n2, k, j, i));
+        if (i0 + q < n1) {
+          b[q] = bb ? ro(bb + ox + q) : z;
+          sg[q] = ro(sg0 + ox + q);
           if (!FWD) {
-            exjm[q] = V.ld(0, k, j - 1, i);
-            exkm[q] = V.ld(0, k - 1, j, i);
-            eyA[q] = ro(V.at(1, k, j, i + 1));
-            eyB[q] = ro(V.at(1, k, j, i));
-            eyC[q] = ro(V.at(1, k, j - 1, i + 1));
-            eyD[q] = ro(V.at(1, k, j - 1, i));
-            ezA[q] = ro(V.at(2, k, j, i + 1));
-            ezB[q] = ro(V.at(2, k, j, i));
-            ezC[q] = ro(V.at(2, k - 1, j, i + 1));
-            ezD[q] = ro(V.at(2, k - 1, j, i));
+            exjm[q] = ex0[ox - n1 + q];
+            exkm[q] = ex1[ox + q];
+            eyA[q] = ro(ey0 + oy + q + 1);
+            eyB[q] = ro(ey0 + oy + q);
+            eyC[q] = ro(ey0 + oy - L1 + q + 1);
+            eyD[q] = ro(ey0 + oy - L1 + q);
+            ezA[q] = ro(ez0 + oy + q + 1);
+            ezB[q] = ro(ez0 + oy + q);
+            ezC[q] = ro(ez1 + oy + q + 1);
+            ezD[q] = ro(ez1 + oy + q);
           }
         }
       }
 #pragma unroll
       for (int q = 0; q < VW; q++) {
-        const int i = i0 + q;
-        if (i >= n1) {
+        if (i0 + q >= n1) {
           res[q] = z;
           continue;
         }
@@ -325,7 +347,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
         else      // own row: j+1 is the previous step's value; row k+1 is the neighbour
           v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, eyA[q], eyB[q], eyC[q], eyD[q], res[q], exjm[q], nb[q], exkm[q],
                         ezA[q], ezB[q], ezC[q], ezD[q], b[q], sg[q]);
-        *V.at(0, k, j, i) = v;
+        ex0[ox + q] = v;
         res[q] = v;
       }
     } else {
@@ -369,6 +391,37 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
     Y = rowok ? axis<P>(g.d2, g.d2s, g.r2, g.r2s, j) : Ax<P>{};
     Z = axis_at<P>(g.d3, g.d3s, g.r3, g.r3s, k);
   }
+  // the rows this thread reads and writes (element i is row[i])
+  C* own = nullptr;                                 // this component at (k, j)
+  const C *nxt = nullptr;                           // this component on the next row
+  const C *xa = nullptr, *xb = nullptr;             // Ex rows
+  const C *ya = nullptr, *yb = nullptr, *yc = nullptr, *yd = nullptr;  // the other component's rows
+  const C* bb = nullptr;
+  const R* sg0 = nullptr;
+  if (rowok) {
+    if (COMP == 1) {
+      own = V.row(1, k, j);
+      nxt = V.row(1, k - 1, j);
+      xa = V.row(0, k, j + 1);
+      xb = V.row(0, k, j);
+      ya = V.row(2, k, j + 1);
+      yb = V.row(2, k, j);
+      yc = V.row(2, k - 1, j + 1);
+      yd = V.row(2, k - 1, j);
+      sg0 = g.s22 + ix2(n1, n2, k, j, 0);
+    } else {
+      own = V.row(2, k, j);
+      nxt = V.row(2, k, j - 1);
+      xa = V.row(0, k + 1, j);
+      xb = V.row(0, k, j);
+      ya = V.row(1, k + 1, j);
+      yb = V.row(1, k, j);
+      yc = V.row(1, k + 1, j - 1);
+      yd = V.row(1, k, j - 1);
+      sg0 = g.s33 + ix3(n1, n2, k, j, 0);
+    }
+    bb = V.brow(COMP, k, j);
+  }
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
@@ -387,36 +440,21 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
         if (m < M) {
           const int i = FWD ? 1 + m : M - m;
           X[q] = axis<P>(g.d1, g.d1s, g.r1, g.r1s, i);
-          const int cc = COMP;
-          b[q] = k >= V.vshift ? ro(V.X[cc] + V.idx(cc, k - V.vshift, j, i)) : z;
-          if (COMP == 1) {
-            sg[q] = ro(g.s22 + ix2(n1, n2, k, j, i));
-            xA[q] = ro(V.at(0, k, j + 1, i));
-            xB[q] = ro(V.at(0, k, j, i));
-            xC[q] = ro(V.at(0, k, j + 1, i - 1));
-            xD[q] = ro(V.at(0, k, j, i - 1));
-            if (!FWD) {  // Ez, this row's next position, and the next row's old value
-              yA[q] = ro(V.at(2, k, j + 1, i));
-              yB[q] = ro(V.at(2, k, j, i));
-              yC[q] = ro(V.at(2, k - 1, j + 1, i));
-              yD[q] = ro(V.at(2, k - 1, j, i));
-              own2[q] = V.ld(1, k, j, i - 1);
-              rowold[q] = V.ld(1, k - 1, j, i);
-            }
-          } else {
-            sg[q] = ro(g.s33 + ix3(n1, n2, k, j, i));
-            xA[q] = ro(V.at(0, k + 1, j, i));
-            xB[q] = ro(V.at(0, k, j, i));
-            xC[q] = ro(V.at(0, k + 1, j, i - 1));
-            xD[q] = ro(V.at(0, k, j, i - 1));
-            yA[q] = ro(V.at(1, k + 1, j, i));
-            yB[q] = ro(V.at(1, k, j, i));
-            yC[q] = ro(V.at(1, k + 1, j - 1, i));
-            yD[q] = ro(V.at(1, k, j - 1, i));
-            if (!FWD) {
-              own2[q] = V.ld(2, k, j, i - 1);
-              rowold[q] = V.ld(2, k, j - 1, i);
-            }
+          b[q] = bb ? ro(bb + i) : z;
+          sg[q] = ro(sg0 + i);
+          xA[q] = ro(xa + i);
+          xB[q] = ro(xb + i);
+          xC[q] = ro(xa + i - 1);
+          xD[q] = ro(xb + i - 1);
+          if (COMP == 2 || !FWD) {  // the other component: Ey for Ez, Ez backward for Ey
+            yA[q] = ro(ya + i);
+            yB[q] = ro(yb + i);
+            yC[q] = ro(yc + i);
+            yD[q] = ro(yd + i);
+          }
+          if (!FWD) {  // this row at the next position and the next row: not yet swept
+            own2[q] = own[i - 1];
+            rowold[q] = nxt[i];
           }
         }
       }
@@ -436,7 +474,6 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
           else
             v = upd_ey<P>(sc, g.fvm, X[q], Y, Z, yA[q], yB[q], yC[q], yD[q], nb[q], rowold[q], prev, own2[q], xA[q],
                           xB[q], xC[q], xD[q], b[q], sg[q]);
-          *V.at(1, k, j, i) = v;
         } else {
           if (FWD)
             v = upd_ez<P>(sc, g.fvm, X[q], Y, Z, xA[q], xB[q], xC[q], xD[q], z, prev, z, nb[q], yA[q], yB[q], yC[q],
@@ -444,8 +481,8 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
           else
             v = upd_ez<P>(sc, g.fvm, X[q], Y, Z, xA[q], xB[q], xC[q], xD[q], prev, own2[q], nb[q], rowold[q], yA[q],
                           yB[q], yC[q], yD[q], b[q], sg[q]);
-          *V.at(2, k, j, i) = v;
         }
+        own[i] = v;
         res[q] = v;
         prev = v;
       }
