@@ -1,10 +1,11 @@
 // y = A x: the staggered-grid curl-curl operator of fdfd_apply (fdfd.c:86-205).
 //
-// One CTA owns a BX x BY tile of (i,j) columns plus a one-column halo on the low side
-// (the halo threads only compute H) and marches a chunk of z-planes. At each plane it
-// computes H = curl E / (i omega mu0) for its columns (fdfd.c:125-149), shares it through
-// shared memory, and produces y = curl H - sigma E for the tile (fdfd.c:176-203). H is
-// never written to HBM, so one pass reads x and sigma and writes y.
+// One CTA owns a 31 x BY tile of (i,j) columns plus a one-column and one-row halo on the
+// low sides (the halo threads only compute H) and marches a chunk of z-planes. At each
+// plane it computes H = curl E / (i omega mu0) for its columns (fdfd.c:125-149), trades
+// the neighbouring values by warp shuffles and shared memory, and produces
+// y = curl H - sigma E for the tile (fdfd.c:176-203). H is never written to HBM, so one
+// pass reads x and sigma and writes y.
 //
 // With the airwave boundary (airbc=1) the k=0 rows of bx/by use the ghost fields
 // Hx(z=-dz/2), Hy(z=-dz/2) that the airwave pipeline derives from Hz(z=0)
@@ -41,18 +42,24 @@ __device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __r
   }
 }
 
-template <class P, int BX, int BY>
-__global__ void __launch_bounds__((BX + 1) * (BY + 1))
+// One warp per j row and one lane per i column: lanes cover i = 31*bx - 1 .. 31*bx + 30
+// (lane 0 is the i-1 halo), warps cover j = BY*by - 1 .. BY*by + BY - 1 (warp 0 is the
+// j-1 halo). Each thread keeps Ex and Ey of the next plane in registers for the plane
+// after, gets the i+1 neighbours of Ey and Ez from the next lane, the i-1 neighbours of
+// Hy and Hz from the previous lane, and the j-1 neighbours of Hx and Hz from the
+// previous warp through shared memory (double-buffered by plane parity, one barrier per
+// plane). H is evaluated exactly as in h_at, so complex128 results keep their bits.
+template <class P, int BY>
+__global__ void __launch_bounds__(32 * (BY + 1))
 k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
        typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
        const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list)
 {
   typedef typename P::C C;
-  typedef typename P::R R;
-  __shared__ C sHx[BY + 1][BX + 1], sHy[BY + 1][BX + 1], sHz[BY + 1][BX + 1];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i = blockIdx.x * BX + tx - 1;
-  const int j = blockIdx.y * BY + ty - 1;
+  __shared__ C sHx[2][BY + 1][32], sHz[2][BY + 1][32];
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const int i = blockIdx.x * 31 + lane - 1;
+  const int j = blockIdx.y * BY + w - 1;
   const int slot = blockIdx.z / nkc, kc = blockIdx.z % nkc;
   const int sys = sys_list ? sys_list[slot] : slot;
   const int n1 = g.n1, n2 = g.n2, n3 = g.n3, ks = g.kstart;
@@ -67,55 +74,99 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
   const C* ghy = GHY ? GHY + (size_t)slot * n1 * (n2 + 1) : nullptr;
   const int kb = kc * kchunk;
   const int ke = min(n3 + 1, kb + kchunk);
-  const bool interior = tx >= 1 && ty >= 1 && i <= n1 && j <= n2;
+  const bool inside = i >= 0 && j >= 0 && i <= n1 && j <= n2;  // H is zero outside
+  const bool interior = lane >= 1 && w >= 1 && inside;        // this thread writes y
+  const C z = czero<P>();
+  // which of E this column has (index ranges of the three components)
+  const bool hasEx = inside && i < n1, hasEy = inside && j < n2, hasEz = inside;
+  const bool hasExj = inside && i < n1 && j < n2;  // Ex(k, j+1, i) exists
+  const bool hasEzj = inside && j < n2;            // Ez(k, j+1, i) exists
 
-  C pHx = czero<P>(), pHy = czero<P>(), hx, hy, hz;
+  C pHx = z, pHy = z, hx, hy, hz;
   if (kb > 0) {
     h_at<P>(g, Ex, Ey, Ez, iwmu, kb - 1, j, i, hx, hy, hz);
     pHx = hx;
     pHy = hy;
   }
+  C exk = hasEx && kb <= n3 ? Ex[ix1(n1, n2, kb, j, i)] : z;
+  C eyk = hasEy && kb <= n3 ? Ey[ix2(n1, n2, kb, j, i)] : z;
   for (int k = kb; k < ke; k++) {
-    h_at<P>(g, Ex, Ey, Ez, iwmu, k, j, i, hx, hy, hz);
-    sHx[ty][tx] = hx;
-    sHy[ty][tx] = hy;
-    sHz[ty][tx] = hz;
+    const int kf = k + ks;
+    const int pb = k & 1;
+    // this plane's E: Ex, Ey carried; Ez, the j+1 neighbours and the next plane loaded
+    const C ez = hasEz && k < n3 ? Ez[ix3(n1, n2, k, j, i)] : z;
+    const C ezj = hasEzj && k < n3 ? Ez[ix3(n1, n2, k, j + 1, i)] : z;
+    const C exj = hasExj ? Ex[ix1(n1, n2, k, j + 1, i)] : z;
+    const C ex1 = hasEx && k < n3 ? Ex[ix1(n1, n2, k + 1, j, i)] : z;
+    const C ey1 = hasEy && k < n3 ? Ey[ix2(n1, n2, k + 1, j, i)] : z;
+    C ezi, eyi;  // Ez(k, j, i+1), Ey(k, j, i+1): the next lane's, loaded by the last lane
+    ezi.x = __shfl_down_sync(0xffffffffu, ez.x, 1);
+    ezi.y = __shfl_down_sync(0xffffffffu, ez.y, 1);
+    eyi.x = __shfl_down_sync(0xffffffffu, eyk.x, 1);
+    eyi.y = __shfl_down_sync(0xffffffffu, eyk.y, 1);
+    if (lane == 31) {
+      ezi = inside && i < n1 && k < n3 ? Ez[ix3(n1, n2, k, j, i + 1)] : z;
+      eyi = inside && i < n1 && j < n2 ? Ey[ix2(n1, n2, k, j, i + 1)] : z;
+    }
+    // H at (k, j, i), the operations of h_at
+    hx = hy = hz = z;
+    if (inside) {
+      if (j < n2 && k < n3) {
+        C t1 = cdivs<P>(csub<P>(ezj, ez), g.d2s[j], g.r2s[j]);
+        C t2 = cdivs<P>(csub<P>(ey1, eyk), g.d3s[kf], g.r3s[kf]);
+        hx = cmul<P>(csub<P>(t1, t2), iwmu);
+      }
+      if (i < n1 && k < n3) {
+        C t1 = cdivs<P>(csub<P>(ex1, exk), g.d3s[kf], g.r3s[kf]);
+        C t2 = cdivs<P>(csub<P>(ezi, ez), g.d1s[i], g.r1s[i]);
+        hy = cmul<P>(csub<P>(t1, t2), iwmu);
+      }
+      if (i < n1 && j < n2) {
+        C t1 = cdivs<P>(csub<P>(eyi, eyk), g.d1s[i], g.r1s[i]);
+        C t2 = cdivs<P>(csub<P>(exj, exk), g.d2s[j], g.r2s[j]);
+        hz = cmul<P>(csub<P>(t1, t2), iwmu);
+      }
+    }
+    sHx[pb][w][lane] = hx;
+    sHz[pb][w][lane] = hz;
+    C hyl, hzl;  // Hy(k, j, i-1), Hz(k, j, i-1) from the previous lane
+    hyl.x = __shfl_up_sync(0xffffffffu, hy.x, 1);
+    hyl.y = __shfl_up_sync(0xffffffffu, hy.y, 1);
+    hzl.x = __shfl_up_sync(0xffffffffu, hz.x, 1);
+    hzl.y = __shfl_up_sync(0xffffffffu, hz.y, 1);
     __syncthreads();
     if (interior) {
-      const int kf = k + ks;
+      const C hxd = sHx[pb][w - 1][lane], hzd = sHz[pb][w - 1][lane];  // at j-1
       if (i < n1) {  // bx
-        C r = czero<P>();
+        C r = z;
         const bool in = j >= 1 && j <= n2 - 1 && ((k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc));
         if (in) {
           C hyb = k >= 1 ? pHy : ghy[i + (long)n1 * j];
-          C t1 = cdivs<P>(csub<P>(hz, sHz[ty - 1][tx]), g.d2[j], g.r2[j]);
+          C t1 = cdivs<P>(csub<P>(hz, hzd), g.d2[j], g.r2[j]);
           C t2 = cdivs<P>(csub<P>(hy, hyb), g.d3[kf], g.r3[kf]);
-          long p = ix1(n1, n2, k, j, i);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s11[ix1(n1, n2, kf, j, i)], Ex[p]));
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s11[ix1(n1, n2, kf, j, i)], exk));
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[kf]), iom));
         }
         bx[ix1(n1, n2, k, j, i)] = r;
       }
       if (j < n2) {  // by
-        C r = czero<P>();
+        C r = z;
         const bool in = i >= 1 && i <= n1 - 1 && ((k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc));
         if (in) {
           C hxb = k >= 1 ? pHx : ghx[i + (long)(n1 + 1) * j];
           C t1 = cdivs<P>(csub<P>(hx, hxb), g.d3[kf], g.r3[kf]);
-          C t2 = cdivs<P>(csub<P>(hz, sHz[ty][tx - 1]), g.d1[i], g.r1[i]);
-          long p = ix2(n1, n2, k, j, i);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s22[ix2(n1, n2, kf, j, i)], Ey[p]));
+          C t2 = cdivs<P>(csub<P>(hz, hzl), g.d1[i], g.r1[i]);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s22[ix2(n1, n2, kf, j, i)], eyk));
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1[i], g.d2s[j]), g.d3[kf]), iom));
         }
         by[ix2(n1, n2, k, j, i)] = r;
       }
       if (k < n3) {  // bz
-        C r = czero<P>();
+        C r = z;
         if (i >= 1 && i <= n1 - 1 && j >= 1 && j <= n2 - 1) {
-          C t1 = cdivs<P>(csub<P>(hy, sHy[ty][tx - 1]), g.d1[i], g.r1[i]);
-          C t2 = cdivs<P>(csub<P>(hx, sHx[ty - 1][tx]), g.d2[j], g.r2[j]);
-          long p = ix3(n1, n2, k, j, i);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s33[ix3(n1, n2, kf, j, i)], Ez[p]));
+          C t1 = cdivs<P>(csub<P>(hy, hyl), g.d1[i], g.r1[i]);
+          C t2 = cdivs<P>(csub<P>(hx, hxd), g.d2[j], g.r2[j]);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s33[ix3(n1, n2, kf, j, i)], ez));
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1[i], g.d2[j]), g.d3s[kf]), iom));
         }
         bz[ix3(n1, n2, k, j, i)] = r;
@@ -123,9 +174,9 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
     }
     pHx = hx;
     pHy = hy;
-    __syncthreads();
+    exk = ex1;
+    eyk = ey1;
   }
-  (void)sizeof(R);
 }
 
 // Hz on the plane k=0 (operator grid) for the airwave: out[sys][j][i], i<n1, j<n2
@@ -150,17 +201,19 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
                  const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
                  cudaStream_t st)
 {
-  constexpr int BX = 32, BY = 8;
-  dim3 blk(BX + 1, BY + 1);
-  int gx = (g.n1 + 1 + BX - 1) / BX, gy = (g.n2 + 1 + BY - 1) / BY;
-  long base = (long)gx * gy * nsys;
+  constexpr int BY = 8;
+  dim3 blk(32, BY + 1);
+  const int gx = (g.n1 + 1 + 30) / 31, gy = (g.n2 + 1 + BY - 1) / BY;
+  const long base = (long)gx * gy * nsys;
+  // split the planes into chunks until about four CTAs per SM are in the grid
   int nkc = (int)((4L * 152 + base - 1) / base);
+  const int maxc = (g.n3 + 1) / 8 > 0 ? (g.n3 + 1) / 8 : 1;  // chunks of at least 8 planes
+  if (nkc > maxc) nkc = maxc;
   if (nkc < 1) nkc = 1;
-  if (nkc > (g.n3 + 1) / 4) nkc = (g.n3 + 1) / 4 > 0 ? (g.n3 + 1) / 4 : 1;
-  int kchunk = (g.n3 + 1 + nkc - 1) / nkc;
+  const int kchunk = (g.n3 + 1 + nkc - 1) / nkc;
   nkc = (g.n3 + 1 + kchunk - 1) / kchunk;
   dim3 grd(gx, gy, nsys * nkc);
-  count_launch(), k_fdfd<P, BX, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
+  count_launch(), k_fdfd<P, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
 }
 
 template <class P>
