@@ -48,14 +48,17 @@ __device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __r
 // after, gets the i+1 neighbours of Ey and Ez from the next lane, the i-1 neighbours of
 // Hy and Hz from the previous lane, and the j-1 neighbours of Hx and Hz from the
 // previous warp through shared memory (double-buffered by plane parity, one barrier per
-// plane). H is evaluated exactly as in h_at, so complex128 results keep their bits.
+// plane). Its column's spacings stay in registers and its element offsets advance by one
+// plane stride per plane; the plane's spacings are uniform loads. H is evaluated exactly
+// as in h_at, so complex128 results keep their bits.
 template <class P, int BY>
-__global__ void __launch_bounds__(32 * (BY + 1))
+__global__ void __launch_bounds__(32 * (BY + 1), P::exact ? 2 : 3)
 k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
        typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
        const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list)
 {
   typedef typename P::C C;
+  typedef typename P::R R;
   __shared__ C sHx[2][BY + 1][32], sHz[2][BY + 1][32];
   const int lane = threadIdx.x, w = threadIdx.y;
   const int i = blockIdx.x * 31 + lane - 1;
@@ -77,10 +80,23 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
   const bool inside = i >= 0 && j >= 0 && i <= n1 && j <= n2;  // H is zero outside
   const bool interior = lane >= 1 && w >= 1 && inside;        // this thread writes y
   const C z = czero<P>();
-  // which of E this column has (index ranges of the three components)
-  const bool hasEx = inside && i < n1, hasEy = inside && j < n2, hasEz = inside;
-  const bool hasExj = inside && i < n1 && j < n2;  // Ex(k, j+1, i) exists
-  const bool hasEzj = inside && j < n2;            // Ez(k, j+1, i) exists
+  const bool hasEx = inside && i < n1, hasEy = inside && j < n2;
+  const bool hasExj = hasEx && j < n2;  // Ex(k, j+1, i) exists
+  // the column's spacings
+  const int ic = inside ? i : 0, jc = inside ? j : 0;
+  const R d1s = g.d1s[ic], r1s = g.r1s[ic], d1 = g.d1[ic], r1 = g.r1[ic];
+  const R d2s = g.d2s[jc], r2s = g.r2s[jc], d2 = g.d2[jc], r2 = g.r2[jc];
+  // which outputs this column has, apart from the plane condition
+  const bool outX = interior && i < n1, outY = interior && j < n2, outZ = interior;
+  const bool inX = j >= 1 && j <= n2 - 1, inY = i >= 1 && i <= n1 - 1, inZ = inX && inY;
+  // element offsets at plane k (the same for x, y and, plane-shifted, for sigma)
+  const long sEx = (long)n1 * (n2 + 1), sEy = (long)(n1 + 1) * n2, sEz = (long)(n1 + 1) * (n2 + 1);
+  long oEx = inside ? ix1(n1, n2, kb, j, i) : 0;
+  long oEy = inside ? ix2(n1, n2, kb, j, i) : 0;
+  long oEz = inside ? ix3(n1, n2, kb, j, i) : 0;
+  const R* s11 = g.s11 + ks * sEx;
+  const R* s22 = g.s22 + ks * sEy;
+  const R* s33 = g.s33 + ks * sEz;
 
   C pHx = z, pHy = z, hx, hy, hz;
   if (kb > 0) {
@@ -88,44 +104,44 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
     pHx = hx;
     pHy = hy;
   }
-  C exk = hasEx && kb <= n3 ? Ex[ix1(n1, n2, kb, j, i)] : z;
-  C eyk = hasEy && kb <= n3 ? Ey[ix2(n1, n2, kb, j, i)] : z;
-  for (int k = kb; k < ke; k++) {
+  C exk = hasEx && kb <= n3 ? Ex[oEx] : z;
+  C eyk = hasEy && kb <= n3 ? Ey[oEy] : z;
+  for (int k = kb; k < ke; k++, oEx += sEx, oEy += sEy, oEz += sEz) {
     const int kf = k + ks;
     const int pb = k & 1;
+    const bool kin = k < n3;
+    const R d3s = g.d3s[kf], r3s = g.r3s[kf], d3 = g.d3[kf], r3 = g.r3[kf];
     // this plane's E: Ex, Ey carried; Ez, the j+1 neighbours and the next plane loaded
-    const C ez = hasEz && k < n3 ? Ez[ix3(n1, n2, k, j, i)] : z;
-    const C ezj = hasEzj && k < n3 ? Ez[ix3(n1, n2, k, j + 1, i)] : z;
-    const C exj = hasExj ? Ex[ix1(n1, n2, k, j + 1, i)] : z;
-    const C ex1 = hasEx && k < n3 ? Ex[ix1(n1, n2, k + 1, j, i)] : z;
-    const C ey1 = hasEy && k < n3 ? Ey[ix2(n1, n2, k + 1, j, i)] : z;
+    const C ez = inside && kin ? Ez[oEz] : z;
+    const C ezj = hasEy && kin ? Ez[oEz + (n1 + 1)] : z;
+    const C exj = hasExj ? Ex[oEx + n1] : z;
+    const C ex1 = hasEx && kin ? Ex[oEx + sEx] : z;
+    const C ey1 = hasEy && kin ? Ey[oEy + sEy] : z;
     C ezi, eyi;  // Ez(k, j, i+1), Ey(k, j, i+1): the next lane's, loaded by the last lane
     ezi.x = __shfl_down_sync(0xffffffffu, ez.x, 1);
     ezi.y = __shfl_down_sync(0xffffffffu, ez.y, 1);
     eyi.x = __shfl_down_sync(0xffffffffu, eyk.x, 1);
     eyi.y = __shfl_down_sync(0xffffffffu, eyk.y, 1);
     if (lane == 31) {
-      ezi = inside && i < n1 && k < n3 ? Ez[ix3(n1, n2, k, j, i + 1)] : z;
-      eyi = inside && i < n1 && j < n2 ? Ey[ix2(n1, n2, k, j, i + 1)] : z;
+      ezi = hasEx && kin ? Ez[oEz + 1] : z;
+      eyi = hasExj ? Ey[oEy + 1] : z;
     }
     // H at (k, j, i), the operations of h_at
     hx = hy = hz = z;
-    if (inside) {
-      if (j < n2 && k < n3) {
-        C t1 = cdivs<P>(csub<P>(ezj, ez), g.d2s[j], g.r2s[j]);
-        C t2 = cdivs<P>(csub<P>(ey1, eyk), g.d3s[kf], g.r3s[kf]);
-        hx = cmul<P>(csub<P>(t1, t2), iwmu);
-      }
-      if (i < n1 && k < n3) {
-        C t1 = cdivs<P>(csub<P>(ex1, exk), g.d3s[kf], g.r3s[kf]);
-        C t2 = cdivs<P>(csub<P>(ezi, ez), g.d1s[i], g.r1s[i]);
-        hy = cmul<P>(csub<P>(t1, t2), iwmu);
-      }
-      if (i < n1 && j < n2) {
-        C t1 = cdivs<P>(csub<P>(eyi, eyk), g.d1s[i], g.r1s[i]);
-        C t2 = cdivs<P>(csub<P>(exj, exk), g.d2s[j], g.r2s[j]);
-        hz = cmul<P>(csub<P>(t1, t2), iwmu);
-      }
+    if (hasEy && kin) {
+      C t1 = cdivs<P>(csub<P>(ezj, ez), d2s, r2s);
+      C t2 = cdivs<P>(csub<P>(ey1, eyk), d3s, r3s);
+      hx = cmul<P>(csub<P>(t1, t2), iwmu);
+    }
+    if (hasEx && kin) {
+      C t1 = cdivs<P>(csub<P>(ex1, exk), d3s, r3s);
+      C t2 = cdivs<P>(csub<P>(ezi, ez), d1s, r1s);
+      hy = cmul<P>(csub<P>(t1, t2), iwmu);
+    }
+    if (hasExj) {
+      C t1 = cdivs<P>(csub<P>(eyi, eyk), d1s, r1s);
+      C t2 = cdivs<P>(csub<P>(exj, exk), d2s, r2s);
+      hz = cmul<P>(csub<P>(t1, t2), iwmu);
     }
     sHx[pb][w][lane] = hx;
     sHz[pb][w][lane] = hz;
@@ -137,39 +153,38 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
     __syncthreads();
     if (interior) {
       const C hxd = sHx[pb][w - 1][lane], hzd = sHz[pb][w - 1][lane];  // at j-1
-      if (i < n1) {  // bx
+      const bool kxy = (k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc);
+      if (outX) {  // bx
         C r = z;
-        const bool in = j >= 1 && j <= n2 - 1 && ((k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc));
-        if (in) {
+        if (inX && kxy) {
           C hyb = k >= 1 ? pHy : ghy[i + (long)n1 * j];
-          C t1 = cdivs<P>(csub<P>(hz, hzd), g.d2[j], g.r2[j]);
-          C t2 = cdivs<P>(csub<P>(hy, hyb), g.d3[kf], g.r3[kf]);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s11[ix1(n1, n2, kf, j, i)], exk));
-          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[kf]), iom));
+          C t1 = cdivs<P>(csub<P>(hz, hzd), d2, r2);
+          C t2 = cdivs<P>(csub<P>(hy, hyb), d3, r3);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(s11[oEx], exk));
+          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1s, d2), d3), iom));
         }
-        bx[ix1(n1, n2, k, j, i)] = r;
+        bx[oEx] = r;
       }
-      if (j < n2) {  // by
+      if (outY) {  // by
         C r = z;
-        const bool in = i >= 1 && i <= n1 - 1 && ((k >= 1 && k <= n3 - 1) || (k == 0 && g.airbc));
-        if (in) {
+        if (inY && kxy) {
           C hxb = k >= 1 ? pHx : ghx[i + (long)(n1 + 1) * j];
-          C t1 = cdivs<P>(csub<P>(hx, hxb), g.d3[kf], g.r3[kf]);
-          C t2 = cdivs<P>(csub<P>(hz, hzl), g.d1[i], g.r1[i]);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s22[ix2(n1, n2, kf, j, i)], eyk));
-          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1[i], g.d2s[j]), g.d3[kf]), iom));
+          C t1 = cdivs<P>(csub<P>(hx, hxb), d3, r3);
+          C t2 = cdivs<P>(csub<P>(hz, hzl), d1, r1);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(s22[oEy], eyk));
+          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1, d2s), d3), iom));
         }
-        by[ix2(n1, n2, k, j, i)] = r;
+        by[oEy] = r;
       }
-      if (k < n3) {  // bz
+      if (outZ && kin) {  // bz
         C r = z;
-        if (i >= 1 && i <= n1 - 1 && j >= 1 && j <= n2 - 1) {
-          C t1 = cdivs<P>(csub<P>(hy, hyl), g.d1[i], g.r1[i]);
-          C t2 = cdivs<P>(csub<P>(hx, hxd), g.d2[j], g.r2[j]);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(g.s33[ix3(n1, n2, kf, j, i)], ez));
-          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(g.d1[i], g.d2[j]), g.d3s[kf]), iom));
+        if (inZ) {
+          C t1 = cdivs<P>(csub<P>(hy, hyl), d1, r1);
+          C t2 = cdivs<P>(csub<P>(hx, hxd), d2, r2);
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(s33[oEz], ez));
+          if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1, d2), d3s), iom));
         }
-        bz[ix3(n1, n2, k, j, i)] = r;
+        bz[oEz] = r;
       }
     }
     pHx = hx;
