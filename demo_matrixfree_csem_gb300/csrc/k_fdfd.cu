@@ -52,7 +52,7 @@ __device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __r
 // plane stride per plane; the plane's spacings are uniform loads. H is evaluated exactly
 // as in h_at, so complex128 results keep their bits.
 template <class P, int BY>
-__global__ void __launch_bounds__(32 * (BY + 1), P::exact ? 2 : 3)
+__global__ void __launch_bounds__(32 * (BY + 1), P::exact ? 1 : 2)
 k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
        typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
        const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list)
@@ -106,17 +106,34 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
   }
   C exk = hasEx && kb <= n3 ? Ex[oEx] : z;
   C eyk = hasEy && kb <= n3 ? Ey[oEy] : z;
+  // the loads of one plane: Ez, the j+1 neighbours, Ex and Ey of the plane above, and
+  // sigma; issued one plane ahead of their use
+  struct PlaneIn {
+    C ez, ezj, exj, ex1, ey1;
+    R s1, s2, s3;
+  };
+  auto load_plane = [&](int k, long oX, long oY, long oZ) {
+    PlaneIn p;
+    const bool kin = k < n3;
+    p.ez = inside && kin ? Ez[oZ] : z;
+    p.ezj = hasEy && kin ? Ez[oZ + (n1 + 1)] : z;
+    p.exj = hasExj ? Ex[oX + n1] : z;
+    p.ex1 = hasEx && kin ? Ex[oX + sEx] : z;
+    p.ey1 = hasEy && kin ? Ey[oY + sEy] : z;
+    p.s1 = outX ? s11[oX] : R(0);
+    p.s2 = outY ? s22[oY] : R(0);
+    p.s3 = outZ && kin ? s33[oZ] : R(0);
+    return p;
+  };
+  PlaneIn nxt = load_plane(kb, oEx, oEy, oEz);
   for (int k = kb; k < ke; k++, oEx += sEx, oEy += sEy, oEz += sEz) {
     const int kf = k + ks;
     const int pb = k & 1;
     const bool kin = k < n3;
+    const PlaneIn cur = nxt;
+    if (k + 1 < ke) nxt = load_plane(k + 1, oEx + sEx, oEy + sEy, oEz + sEz);
     const R d3s = g.d3s[kf], r3s = g.r3s[kf], d3 = g.d3[kf], r3 = g.r3[kf];
-    // this plane's E: Ex, Ey carried; Ez, the j+1 neighbours and the next plane loaded
-    const C ez = inside && kin ? Ez[oEz] : z;
-    const C ezj = hasEy && kin ? Ez[oEz + (n1 + 1)] : z;
-    const C exj = hasExj ? Ex[oEx + n1] : z;
-    const C ex1 = hasEx && kin ? Ex[oEx + sEx] : z;
-    const C ey1 = hasEy && kin ? Ey[oEy + sEy] : z;
+    const C ez = cur.ez, ezj = cur.ezj, exj = cur.exj, ex1 = cur.ex1, ey1 = cur.ey1;
     C ezi, eyi;  // Ez(k, j, i+1), Ey(k, j, i+1): the next lane's, loaded by the last lane
     ezi.x = __shfl_down_sync(0xffffffffu, ez.x, 1);
     ezi.y = __shfl_down_sync(0xffffffffu, ez.y, 1);
@@ -160,7 +177,7 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
           C hyb = k >= 1 ? pHy : ghy[i + (long)n1 * j];
           C t1 = cdivs<P>(csub<P>(hz, hzd), d2, r2);
           C t2 = cdivs<P>(csub<P>(hy, hyb), d3, r3);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(s11[oEx], exk));
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(cur.s1, exk));
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1s, d2), d3), iom));
         }
         bx[oEx] = r;
@@ -171,7 +188,7 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
           C hxb = k >= 1 ? pHx : ghx[i + (long)(n1 + 1) * j];
           C t1 = cdivs<P>(csub<P>(hx, hxb), d3, r3);
           C t2 = cdivs<P>(csub<P>(hz, hzl), d1, r1);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(s22[oEy], eyk));
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(cur.s2, eyk));
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1, d2s), d3), iom));
         }
         by[oEy] = r;
@@ -181,7 +198,7 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
         if (inZ) {
           C t1 = cdivs<P>(csub<P>(hy, hyl), d1, r1);
           C t2 = cdivs<P>(csub<P>(hx, hxd), d2, r2);
-          r = csub<P>(csub<P>(t1, t2), rmul<P>(s33[oEz], ez));
+          r = csub<P>(csub<P>(t1, t2), rmul<P>(cur.s3, ez));
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1, d2), d3s), iom));
         }
         bz[oEz] = r;
