@@ -25,7 +25,6 @@
 // complex quotient.
 #include "csem_cuda.cuh"
 #include "engine.h"
-#include "engine_model.h"
 
 namespace csem {
 
@@ -264,16 +263,9 @@ __device__ __forceinline__ void hand_over(const C (&res)[VW], C (*hand)[2][VW], 
 
 }  // namespace
 
-// A CTA sweeps `nline` consecutive independent lines one after the other, each thread
-// moving on to its row of the next line as soon as it finished its row of the current
-// one: thread t works on line l, march position c at step l * (march positions) + c + t.
-// The row before it reached that (line, position) one step earlier, so the hand-over is
-// unchanged, and the pipeline fills and drains once per CTA instead of once per line.
-
-// Ex sweep: rows k, march j, VW consecutive i per thread; lines are groups of VW i.
-// grid (line groups, systems)
+// Ex sweep: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
 template <class P, bool FWD, int VW>
-__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(SweepP<P> s, int nline)
+__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
@@ -282,8 +274,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
   const int n1 = g.n1, n2 = g.n2, nK = s.nK;
-  const int NL = (n1 + VW - 1) / VW;
-  const int l0 = blockIdx.x * nline, nl = min(nline, NL - l0);
+  const int i0 = blockIdx.x * VW;
   const View<P> V = view_of<P>(s, slot, sys);
   const SysScal<P> sc = s.scal[sys];
   const C z = czero<P>();
@@ -291,48 +282,35 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
   const int rr = threadIdx.x;
   const bool rowok = rr < R_;
   const int k = FWD ? 1 + rr : R_ - rr;
+  // spacings fixed for this thread: k (row) and the VW i's
   const Ax<P> Z = rowok ? axis<P>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<P>{};
-  // the thread's planes at i = 0; row j is j * row_len
-  C* ex0b = nullptr;
-  const C *ex1b = nullptr, *ey0b = nullptr, *ez0b = nullptr, *ez1b = nullptr, *bbb = nullptr;
-  const R* sg0b = nullptr;
-  if (rowok) {
-    ex0b = V.row(0, k, 0);
-    ex1b = V.row(0, k - 1, 0);
-    ey0b = V.row(1, k, 0);
-    ez0b = V.row(2, k, 0);
-    ez1b = V.row(2, k - 1, 0);
-    bbb = V.brow(0, k, 0);
-    sg0b = g.s11 + ix1(n1, n2, k, 0, 0);
-  }
-  const int L1 = n1 + 1;
-  // the current line's state
-  int i0 = 0;
+  Ax<P> X[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++)
+    X[q] = i0 + q < n1 ? axis_at<P>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<P>{};
+  // planes this thread reads and writes, offset to its first i; row j is j * row_len
   C* ex0 = nullptr;
   const C *ex1 = nullptr, *ey0 = nullptr, *ez0 = nullptr, *ez1 = nullptr, *bb = nullptr;
   const R* sg0 = nullptr;
-  Ax<P> X[VW];
+  if (rowok) {
+    ex0 = V.row(0, k, 0) + i0;
+    ex1 = V.row(0, k - 1, 0) + i0;
+    ey0 = V.row(1, k, 0) + i0;
+    ez0 = V.row(2, k, 0) + i0;
+    ez1 = V.row(2, k - 1, 0) + i0;
+    bb = V.brow(0, k, 0);
+    if (bb) bb += i0;
+    sg0 = g.s11 + ix1(n1, n2, k, 0, i0);
+  }
+  const int L1 = n1 + 1;
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
-  int l = 0, c = -rr;  // line and march position of this thread at step T
-  for (int T = 0; T < nl * M + R_ - 1; T++) {
+  for (int T = 0; T < M + R_ - 1; T++) {
     C nb[VW];
     neighbours<VW, C>(res, nb, hand, T);
-    if (rowok && c >= 0 && l < nl) {
-      if (c == 0) {  // a new line
-        i0 = (l0 + l) * VW;
-        ex0 = ex0b + i0;
-        ex1 = ex1b + i0;
-        ey0 = ey0b + i0;
-        ez0 = ez0b + i0;
-        ez1 = ez1b + i0;
-        bb = bbb ? bbb + i0 : nullptr;
-        sg0 = sg0b + i0;
-#pragma unroll
-        for (int q = 0; q < VW; q++)
-          X[q] = i0 + q < n1 ? axis_at<P>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<P>{};
-      }
+    const int c = T - rr;
+    if (rowok && c >= 0 && c < M) {
       const int j = FWD ? 1 + c : M - c;
       const Ax<P> Y = axis<P>(g.d2, g.d2s, g.r2, g.r2s, j);
       const int ox = j * n1, oy = j * L1;
@@ -363,12 +341,11 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
           res[q] = z;
           continue;
         }
-        const C own = c > 0 ? res[q] : z;  // own row at the previous position; boundary at a line start
         C v;
         if (FWD)  // own row: j-1 is the previous step's value; row k-1 is the neighbour
-          v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, z, z, z, z, z, own, z, nb[q], z, z, z, z, b[q], sg[q]);
+          v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, z, z, z, z, z, res[q], z, nb[q], z, z, z, z, b[q], sg[q]);
         else      // own row: j+1 is the previous step's value; row k+1 is the neighbour
-          v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, eyA[q], eyB[q], eyC[q], eyD[q], own, exjm[q], nb[q], exkm[q],
+          v = upd_ex<P>(sc, g.fvm, X[q], Y, Z, eyA[q], eyB[q], eyC[q], eyD[q], res[q], exjm[q], nb[q], exkm[q],
                         ezA[q], ezB[q], ezC[q], ezD[q], b[q], sg[q]);
         ex0[ox + q] = v;
         res[q] = v;
@@ -378,17 +355,13 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
       for (int q = 0; q < VW; q++) res[q] = z;
     }
     hand_over<VW, C>(res, hand, T);
-    if (++c == M) {
-      c = 0;
-      ++l;
-    }
   }
 }
 
-// Ey (COMP 1: lines j, rows k) / Ez (COMP 2: lines k, rows j) sweeps, march i in chunks
-// of VW. grid (line groups, systems)
+// Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j) sweeps, march i in chunks
+// of VW. grid (lines, systems)
 template <class P, int COMP, bool FWD, int VW>
-__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(SweepP<P> s, int nline)
+__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
@@ -397,8 +370,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
   const int n1 = g.n1, n2 = g.n2, nK = s.nK;
-  const int NL = COMP == 1 ? n2 : nK;  // lines j (Ey) or k (Ez)
-  const int l0 = blockIdx.x * nline, nl = min(nline, NL - l0);
+  const int line = blockIdx.x;  // j (Ey) or k (Ez)
   const View<P> V = view_of<P>(s, slot, sys);
   const SysScal<P> sc = s.scal[sys];
   const C z = czero<P>();
@@ -408,59 +380,56 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
   const int rr = threadIdx.x;
   const bool rowok = rr < R_;
   const int r = FWD ? 1 + rr : R_ - rr;
-  // the row's spacings (k for Ey, j for Ez) are fixed for this thread
-  const Ax<P> Rw = rowok ? (COMP == 1 ? axis<P>(g.d3, g.d3s, g.r3, g.r3s, r) : axis<P>(g.d2, g.d2s, g.r2, g.r2s, r))
-                         : Ax<P>{};
-  // the current line's state: its spacings and the rows this thread reads and writes
-  int k = 0, j = 0;
+  const int k = COMP == 1 ? r : line;
+  const int j = COMP == 1 ? line : r;
+  // spacings fixed for this thread: the line's and the row's
   Ax<P> Y, Z;
+  if (COMP == 1) {
+    Y = axis_at<P>(g.d2, g.d2s, g.r2, g.r2s, j);
+    Z = rowok ? axis<P>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<P>{};
+  } else {
+    Y = rowok ? axis<P>(g.d2, g.d2s, g.r2, g.r2s, j) : Ax<P>{};
+    Z = axis_at<P>(g.d3, g.d3s, g.r3, g.r3s, k);
+  }
+  // the rows this thread reads and writes (element i is row[i])
   C* own = nullptr;                                 // this component at (k, j)
   const C *nxt = nullptr;                           // this component on the next row
   const C *xa = nullptr, *xb = nullptr;             // Ex rows
   const C *ya = nullptr, *yb = nullptr, *yc = nullptr, *yd = nullptr;  // the other component's rows
   const C* bb = nullptr;
   const R* sg0 = nullptr;
+  if (rowok) {
+    if (COMP == 1) {
+      own = V.row(1, k, j);
+      nxt = V.row(1, k - 1, j);
+      xa = V.row(0, k, j + 1);
+      xb = V.row(0, k, j);
+      ya = V.row(2, k, j + 1);
+      yb = V.row(2, k, j);
+      yc = V.row(2, k - 1, j + 1);
+      yd = V.row(2, k - 1, j);
+      sg0 = g.s22 + ix2(n1, n2, k, j, 0);
+    } else {
+      own = V.row(2, k, j);
+      nxt = V.row(2, k, j - 1);
+      xa = V.row(0, k + 1, j);
+      xb = V.row(0, k, j);
+      ya = V.row(1, k + 1, j);
+      yb = V.row(1, k, j);
+      yc = V.row(1, k + 1, j - 1);
+      yd = V.row(1, k, j - 1);
+      sg0 = g.s33 + ix3(n1, n2, k, j, 0);
+    }
+    bb = V.brow(COMP, k, j);
+  }
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
-  int l = 0, c = -rr;  // line and march chunk of this thread at step T
-  for (int T = 0; T < nl * NC + R_ - 1; T++) {
+  for (int T = 0; T < NC + R_ - 1; T++) {
     C nb[VW];
     neighbours<VW, C>(res, nb, hand, T);
-    if (rowok && c >= 0 && l < nl) {
-      if (c == 0) {  // a new line
-        const int line = l0 + l;
-        if (COMP == 1) {
-          k = r;
-          j = line;
-          Y = axis_at<P>(g.d2, g.d2s, g.r2, g.r2s, j);
-          Z = Rw;
-          own = V.row(1, k, j);
-          nxt = V.row(1, k - 1, j);
-          xa = V.row(0, k, j + 1);
-          xb = V.row(0, k, j);
-          ya = V.row(2, k, j + 1);
-          yb = V.row(2, k, j);
-          yc = V.row(2, k - 1, j + 1);
-          yd = V.row(2, k - 1, j);
-          sg0 = g.s22 + ix2(n1, n2, k, j, 0);
-        } else {
-          k = line;
-          j = r;
-          Y = Rw;
-          Z = axis_at<P>(g.d3, g.d3s, g.r3, g.r3s, k);
-          own = V.row(2, k, j);
-          nxt = V.row(2, k, j - 1);
-          xa = V.row(0, k + 1, j);
-          xb = V.row(0, k, j);
-          ya = V.row(1, k + 1, j);
-          yb = V.row(1, k, j);
-          yc = V.row(1, k + 1, j - 1);
-          yd = V.row(1, k, j - 1);
-          sg0 = g.s33 + ix3(n1, n2, k, j, 0);
-        }
-        bb = V.brow(COMP, k, j);
-      }
+    const int c = T - rr;
+    if (rowok && c >= 0 && c < NC) {
       C prev = c > 0 ? res[VW - 1] : z;  // own row at the previous march position
       C b[VW], xA[VW], xB[VW], xC[VW], xD[VW], yA[VW], yB[VW], yC[VW], yD[VW], own2[VW], rowold[VW];
       R sg[VW];
@@ -522,10 +491,6 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
       for (int q = 0; q < VW; q++) res[q] = z;
     }
     hand_over<VW, C>(res, hand, T);
-    if (++c == NC) {
-      c = 0;
-      ++l;
-    }
   }
 }
 
@@ -535,49 +500,25 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
   return rows >= 1 && rows <= MAXROWS && n1 >= 2 && n2 >= 2;
 }
 
-// Lines per CTA: the count that minimises (waves of CTAs) x (steps of one CTA), with the
-// resident CTAs per SM taken from the occupancy calculator.
-template <class K>
-static int lines_per_cta(K kern, int threads, int nlines, int nslot, int steps_per_line, int rows)
-{
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    CSEM_CUDA_TRY(cudaGetDevice(&dev));
-    CSEM_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
-  int per_sm = 0;
-  CSEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
-  const long cap = (long)nsm * (per_sm > 0 ? per_sm : 1);
-  int best = 1;
-  double best_t = 1e300;
-  for (int q = 1; q <= nlines; q++) {
-    const long ctas = (long)((nlines + q - 1) / q) * nslot;
-    const double t = (double)((ctas + cap - 1) / cap) * ((double)q * steps_per_line + rows - 1);
-    if (t < best_t * 0.999) {
-      best_t = t;
-      best = q;
-    }
-  }
-  return best;
-}
-
 template <class P, int VW>
 static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st)
 {
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
   const int threads = (rows + 31) / 32 * 32;
-  const int nlines = comp == 0 ? (n1 + VW - 1) / VW : (comp == 1 ? n2 : nK);
-  const int steps = comp == 0 ? n2 - 1 : (n1 - 1 + VW - 1) / VW;
-  auto go = [&](void (*kern)(SweepP<P>, int)) {
-    const int q = lines_per_cta(kern, threads, nlines, nslot, steps, rows);
-    dim3 grd((nlines + q - 1) / q, nslot);
-    count_launch(), kern<<<grd, threads, 0, st>>>(s, q);
-  };
-  if (comp == 0) go(fwd ? k_sweep_ex<P, true, VW> : k_sweep_ex<P, false, VW>);
-  else if (comp == 1) go(fwd ? k_sweep_eyz<P, 1, true, VW> : k_sweep_eyz<P, 1, false, VW>);
-  else go(fwd ? k_sweep_eyz<P, 2, true, VW> : k_sweep_eyz<P, 2, false, VW>);
+  if (comp == 0) {
+    dim3 grd((n1 + VW - 1) / VW, nslot);
+    if (fwd) count_launch(), k_sweep_ex<P, true, VW><<<grd, threads, 0, st>>>(s);
+    else count_launch(), k_sweep_ex<P, false, VW><<<grd, threads, 0, st>>>(s);
+  } else if (comp == 1) {
+    dim3 grd(n2, nslot);
+    if (fwd) count_launch(), k_sweep_eyz<P, 1, true, VW><<<grd, threads, 0, st>>>(s);
+    else count_launch(), k_sweep_eyz<P, 1, false, VW><<<grd, threads, 0, st>>>(s);
+  } else {
+    dim3 grd(nK, nslot);
+    if (fwd) count_launch(), k_sweep_eyz<P, 2, true, VW><<<grd, threads, 0, st>>>(s);
+    else count_launch(), k_sweep_eyz<P, 2, false, VW><<<grd, threads, 0, st>>>(s);
+  }
 }
 
 // vw: points per thread and step (1, 2 or 4; other values select the default, the
