@@ -11,7 +11,8 @@
 // march step per iteration, skewed by one step per row: at step T row t works at march
 // position T - t, so the row before it finished that position at step T - 1. That value
 // arrives by warp shuffle, or through shared memory from the last lane of the previous
-// warp (one __syncthreads per step). The own-row dependency stays in registers and the
+// warp (pairwise named barriers between neighbouring warps). The own-row dependency stays
+// in registers and the
 // sweep's first row depends on the boundary, which is zero. A sweep takes
 // (march positions + rows - 1) steps.
 //
@@ -230,35 +231,62 @@ template <class C> __device__ __forceinline__ C shfl_up(C v)
   return r;
 }
 
+// Hand-over between warps. Warp w's last row feeds warp w+1's first row one step later
+// through a one-slot buffer in shared memory, synchronised pairwise with named barriers
+// (ids 1 + 2w "full" and 2 + 2w "empty", 64 threads each: the producing and the
+// consuming warp), so a warp waits only for its neighbours, never for the whole CTA.
+// At each step T >= 1 the consumer waits on "full", reads and signals "empty"; at each
+// step the producer (from T >= 1 after waiting on "empty", i.e. once the previous value
+// has been read) writes and signals "full". Each barrier generation therefore holds
+// exactly one producer and one consumer operation, and a final wait on "full" after
+// the loop completes the last one (this protocol was checked exhaustively over warp
+// counts and step counts, under arbitrary interleavings, before use).
+__device__ __forceinline__ void nbar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void nbar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
+
 // Value the row before this thread's row produced at the previous step: a shuffle from
-// the previous lane, or shared memory for lane 0 (written by the previous warp's last
-// lane before the barrier); the sweep's first row reads the zero boundary.
+// the previous lane, or the hand-over slot for lane 0; the sweep's first row reads the
+// zero boundary.
 template <int VW, class C>
-__device__ __forceinline__ void neighbours(const C (&res)[VW], C (&nb)[VW], const C (*hand)[2][VW], int T)
+__device__ __forceinline__ void neighbours(const C (&res)[VW], C (&nb)[VW], const C (*hand)[VW], int T)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < VW; q++) nb[q] = shfl_up(res[q]);
-  if (lane == 0) {
+  if (w > 0 && T > 0) {
+    nbar_sync(1 + 2 * (w - 1));  // warp w-1 has written step T-1
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < VW; q++) nb[q] = hand[w - 1][q];
+    }
+    nbar_arrive(2 + 2 * (w - 1));  // the slot may be rewritten
+  } else if (lane == 0) {
 #pragma unroll
     for (int q = 0; q < VW; q++) {
-      C v;
-      v.x = 0;
-      v.y = 0;
-      if (w > 0 && T > 0) v = hand[w - 1][(T - 1) & 1][q];
-      nb[q] = v;
+      nb[q].x = 0;
+      nb[q].y = 0;
     }
   }
 }
 
 template <int VW, class C>
-__device__ __forceinline__ void hand_over(const C (&res)[VW], C (*hand)[2][VW], int T)
+__device__ __forceinline__ void hand_over(const C (&res)[VW], C (*hand)[VW], int T)
 {
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (w + 1 >= nw) return;  // the last warp feeds nobody
+  if (T >= 1) nbar_sync(2 + 2 * w);  // warp w+1 has read step T-1
   if ((threadIdx.x & 31) == 31) {
 #pragma unroll
-    for (int q = 0; q < VW; q++) hand[threadIdx.x >> 5][T & 1][q] = res[q];
+    for (int q = 0; q < VW; q++) hand[w][q] = res[q];
   }
-  __syncthreads();
+  nbar_arrive(1 + 2 * w);
+}
+
+// Completes the last generation of the "full" barriers after the step loop.
+__device__ __forceinline__ void hand_over_finish(int nsteps)
+{
+  const int w = threadIdx.x >> 5;
+  if (w > 0 && nsteps > 0) nbar_sync(1 + 2 * (w - 1));
 }
 
 }  // namespace
@@ -269,7 +297,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
 {
   typedef typename P::C C;
   typedef typename P::R R;
-  __shared__ C hand[MAXROWS / 32][2][VW];
+  __shared__ C hand[MAXROWS / 32][VW];
   const int slot = blockIdx.y;
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
@@ -356,6 +384,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
     }
     hand_over<VW, C>(res, hand, T);
   }
+  hand_over_finish(M + R_ - 1);
 }
 
 // Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j) sweeps, march i in chunks
@@ -365,7 +394,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
 {
   typedef typename P::C C;
   typedef typename P::R R;
-  __shared__ C hand[MAXROWS / 32][2][VW];
+  __shared__ C hand[MAXROWS / 32][VW];
   const int slot = blockIdx.y;
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
@@ -492,6 +521,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(Swe
     }
     hand_over<VW, C>(res, hand, T);
   }
+  hand_over_finish(NC + R_ - 1);
 }
 
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)

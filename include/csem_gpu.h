@@ -159,7 +159,11 @@ void *csem_ctx_stream(csem_ctx *c);
  *   "lusgs_pipelined" 1 (default): one launch per LU-SGS component sweep, rows as a
  *                     lockstep pipeline; 0: one launch per wavefront diagonal;
  *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
- *                     0 for the default (2 complex64, 1 complex128). */
+ *                     0 for the default (2 complex64, 1 complex128).
+ * Solver option (changes iteration counts, not the stopping test):
+ *   "mixed_warm_restart" 1: after each defect correction the complex64 inner BiCGStab
+ *                     continues with the true residual in place of its own;
+ *                     0 (default): it restarts from the new residual. */
 int csem_ctx_set_option(csem_ctx *c, const char *name, int value);
 
 /* ------------------------------------------------------------ timing
