@@ -326,7 +326,7 @@ class _BatchOpts(C.Structure):
 
 
 def solve_batch(ctx: Ctx, freqs, srcs, chsrc=("Ex",), chrec=("Ex", "Ey", "Ez"), rec=None, precision=32, algopt=1,
-                preco=1, niter=1000, tol=1e-8, inner_tol=1e-4, check_every=4, max_outer=30, nrestart=10, mp=30):
+                preco=1, niter=1000, tol=1e-8, inner_tol=0.1, check_every=4, max_outer=30, nrestart=10, mp=30):
     """Solve len(freqs) systems (frequency freqs[s], dipole at srcs[s]) and extract the
     receivers rec ([nrec][5] rows). Returns a dict with dcal [nsys][nchrec][nrec]
     (complex128), iters, outer, status, relres."""

@@ -24,7 +24,7 @@ struct csem_ctx {
   int nmax64 = 0, nmax32 = 0;
   bool lusgs_pipelined = true;
   int lusgs_vw = 0;
-  bool mixed_warm = false;
+  bool autotune = false;
 };
 
 // the context's kernel-schedule options on one operator set
@@ -153,8 +153,8 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     if (value != 0 && value != 1 && value != 2 && value != 4)
       return csem_set_error(CSEM_EINVAL, "lusgs_vw must be 0, 1, 2 or 4");
     c->lusgs_vw = value;
-  } else if (!strcmp(name, "mixed_warm_restart")) {
-    c->mixed_warm = value != 0;
+  } else if (!strcmp(name, "autotune")) {
+    c->autotune = value != 0;
   } else {
     return csem_set_error(CSEM_EINVAL, "unknown option %s", name);
   }
@@ -435,9 +435,9 @@ int csem_solve_batch_host(csem_ctx* c, int nsys, const float* freq, const float*
     mo.max_inner_total = 3 * mo.niter;
     mo.max_outer = opt->max_outer > 0 ? opt->max_outer : 30;
     mo.preco = opt->preco;
-    mo.inner_tol = opt->inner_tol > 0 ? opt->inner_tol : 1e-4;
+    mo.inner_tol = opt->inner_tol > 0 ? opt->inner_tol : 0.1;
     mo.check_every = opt->check_every > 0 ? opt->check_every : 4;
-    mo.warm_restart = c->mixed_warm;
+    mo.autotune = c->autotune;
     std::vector<MixedResult> res;
     B->solve(iom.data(), tol.data(), mo, res);
     B->extract(nchrec, chrec, nrec, rec, dcal);

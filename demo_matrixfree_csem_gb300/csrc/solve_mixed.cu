@@ -51,54 +51,6 @@ __global__ void k_outer_accum(long n, const int* __restrict__ list, const double
   x[o] = xv;
 }
 
-// Warm restart after an inner solve reached its reduction: the true residual replaces the
-// recursive one and the Krylov recursion continues (reliable updates, Sleijpen & van der
-// Vorst 1996). r is renormalised by the new |r| and p, v are rescaled by
-// sig = |r|_old / |r|_new so that they stay in the units of r; r0 is kept.
-__global__ void k_warm_inner(long n, const int* __restrict__ list, const double* __restrict__ rn,
-                             const double* __restrict__ sig, const double2* __restrict__ r64, float2* __restrict__ r,
-                             float2* __restrict__ p, float2* __restrict__ v, float2* __restrict__ d)
-{
-  const int sys = list[blockIdx.y];
-  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const size_t o = (size_t)sys * n + q;
-  const double s = 1.0 / rn[sys];
-  const float g = (float)sig[sys];
-  const double2 rv = r64[o];
-  r[o] = make_float2((float)(rv.x * s), (float)(rv.y * s));
-  const float2 pv = p[o], vv = v[o];
-  p[o] = make_float2(pv.x * g, pv.y * g);
-  v[o] = make_float2(vv.x * g, vv.y * g);
-  d[o] = make_float2(0.f, 0.f);
-}
-
-// beta for the replaced residual: rho_old is rescaled with p and v
-__global__ void k_sc_warm(int nslot, const int* __restrict__ list, KrylovScalars* __restrict__ ks,
-                          const double2* __restrict__ d_rr0, const double2* __restrict__ d_rr,
-                          const double* __restrict__ sig)
-{
-  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot >= nslot) return;
-  const int sys = list[slot];
-  KrylovScalars k = ks[sys];
-  const double rs = d_rr[slot].x;
-  k.rs0 = rs;
-  k.relres = 1.0;
-  k.iter = 0;
-  const double g = sig[sys];
-  const double2 rho_old = make_double2(k.rho_old.x * g, k.rho_old.y * g);
-  const double2 rho_new = d_rr0[slot];
-  if (!(rs > 0.0) || (rho_old.x == 0. && rho_old.y == 0.) || (k.omega.x == 0. && k.omega.y == 0.)) {
-    k.status = ST_BREAKDOWN;  // the host restarts it cold
-  } else {
-    k.beta = cdiv<F64>(cmul<F64>(cdiv<F64>(rho_new, rho_old), k.alpha), k.omega);
-    k.rho_old = rho_new;
-    k.status = isfinite(k.beta.x) && isfinite(k.beta.y) ? ST_RUNNING : ST_BREAKDOWN;
-  }
-  ks[sys] = k;
-}
-
 MixedBatch::MixedBatch(Model* m_, int nsys_, cudaStream_t st_)
     : m(m_), nsys(nsys_), st(st_), n(m_->lE), nblk(dot_blocks(m_->lE)), o64(m_, nsys_, st_), o32(m_, nsys_, st_)
 {
@@ -115,7 +67,6 @@ MixedBatch::MixedBatch(Model* m_, int nsys_, cudaStream_t st_)
   partial.alloc(sizeof(double2) * (size_t)nblk * nsys);
   list.alloc(sizeof(int) * nsys);
   rn.alloc(sizeof(double) * nsys);
-  sig.alloc(sizeof(double) * nsys);
 }
 
 void MixedBatch::inject(const float* src, const double* iom, int nch, const int* ch)
@@ -186,35 +137,6 @@ void MixedBatch::start_inner(const std::vector<int>& g, const std::vector<double
   CSEM_CUDA_TRY(cudaGetLastError());
 }
 
-void MixedBatch::start_inner_warm(const std::vector<int>& g, const std::vector<double>& tol_inner,
-                                  const std::vector<double>& sigma)
-{
-  if (g.empty()) return;
-  std::vector<KrylovScalars> kh(nsys);
-  CSEM_CUDA_TRY(cudaMemcpyAsync(kh.data(), ks.p, sizeof(KrylovScalars) * nsys, cudaMemcpyDeviceToHost, st));
-  CSEM_CUDA_TRY(cudaStreamSynchronize(st));
-  std::vector<double> sg(nsys, 1.0);
-  for (size_t q = 0; q < g.size(); q++) {
-    kh[g[q]].tol = tol_inner[q];
-    sg[g[q]] = sigma[q];
-  }
-  CSEM_CUDA_TRY(cudaMemcpyAsync(ks.p, kh.data(), sizeof(KrylovScalars) * nsys, cudaMemcpyHostToDevice, st));
-  CSEM_CUDA_TRY(cudaMemcpyAsync(sig.p, sg.data(), sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
-  CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, g.data(), sizeof(int) * g.size(), cudaMemcpyHostToDevice, st));
-  const int ng = (int)g.size();
-  const int* dl = list.as<int>();
-  dim3 grd((unsigned)((n + 255) / 256), ng);
-  count_launch(), k_warm_inner<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), sig.as<double>(), r64.as<double2>(),
-                                                     V(0), V(2), V(4), V(7));
-  double2* D = dots.as<double2>();
-  launch_dot<F32>(V(0), V(1), n, n, ng, dl, partial.as<double2>(), nblk, D + 5 * nsys, st);
-  launch_dot<F32>(V(0), V(0), n, n, ng, dl, partial.as<double2>(), nblk, D + 6 * nsys, st);
-  count_launch(), k_sc_warm<<<(ng + 31) / 32, 32, 0, st>>>(ng, dl, ks.as<KrylovScalars>(), D + 5 * nsys, D + 6 * nsys,
-                                                          sig.as<double>());
-  launch_vec<F32>(VEC_P, n, ng, dl, ks.as<KrylovScalars>(), V(0), V(2), V(4), nullptr, nullptr, st);
-  CSEM_CUDA_TRY(cudaGetLastError());
-}
-
 void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first)
 {
   const int ng = (int)g.size();
@@ -234,6 +156,43 @@ void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rn
   CSEM_CUDA_TRY(cudaStreamSynchronize(st));
   for (int q = 0; q < ng; q++) rnorm[g[q]] = std::sqrt(h[q].x);
   CSEM_CUDA_TRY(cudaMemcpyAsync(rn.p, rnorm.data(), sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
+}
+
+// Autotuner of the complex64 LU-SGS schedule: applies the preconditioner to the batch's
+// current vectors once per candidate (points per thread 1, 2, 4 of the lockstep sweeps)
+// after one untimed application each, times it with CUDA events on the solver's stream,
+// and keeps the fastest for the rest of this batch. The scratch vector it writes is
+// overwritten before use by the solve.
+int MixedBatch::autotune_lusgs(int nact, const int* dlist)
+{
+  const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
+  const int cand[3] = {1, 2, 4};
+  cudaEvent_t e0, e1;
+  CSEM_CUDA_TRY(cudaEventCreate(&e0));
+  CSEM_CUDA_TRY(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  int best = 0;
+  const bool saved = o32.pipelined_sweeps;
+  o32.pipelined_sweeps = true;
+  for (int vw : cand) {
+    o32.sweep_vw = vw;
+    o32.apply_lusgs(V(0), V(3), nact, dlist, sc);
+    CSEM_CUDA_TRY(cudaEventRecord(e0, st));
+    o32.apply_lusgs(V(0), V(3), nact, dlist, sc);
+    CSEM_CUDA_TRY(cudaEventRecord(e1, st));
+    CSEM_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CSEM_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = vw;
+    }
+  }
+  o32.pipelined_sweeps = saved;
+  o32.sweep_vw = best;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
 }
 
 void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions& o, std::vector<MixedResult>& res)
@@ -267,6 +226,10 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
     running.push_back(q);
     ti.push_back(std::min(0.5, std::max(o.inner_tol, 0.5 * tol[q])));
   }
+  if (o.autotune && o.preco != PRE_APHI && !running.empty()) {
+    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, running.data(), sizeof(int) * running.size(), cudaMemcpyHostToDevice, st));
+    tuned_vw = autotune_lusgs((int)running.size(), list.as<int>());
+  }
   start_inner(running, ti);
   std::vector<KrylovScalars> kh(nsys);
   inner_launch_iters = 0;
@@ -283,10 +246,9 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
     for (int s : running) (kh[s].status != ST_RUNNING ? done : still).push_back(s);
     if (done.empty()) continue;
     for (int s : done) res[s].inner_iters += kh[s].iter;
-    const std::vector<double> rn_prev = rnorm;
     outer_update(done, rnorm, false);
-    std::vector<int> cold, warm;
-    std::vector<double> cti, wti, wsig;
+    std::vector<int> restart;
+    std::vector<double> rti;
     for (int s : done) {
       res[s].outer += 1;
       const double rel = rnorm[s] / bn[s];
@@ -295,22 +257,13 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
       else if (!std::isfinite(rel)) res[s].status = ST_NONFINITE;
       else if (res[s].inner_iters >= o.max_inner_total || res[s].outer >= o.max_outer) res[s].status = ST_MAXITER;
       else {
-        const double ti = std::min(0.5, std::max(o.inner_tol, 0.5 * tol[s] / rel));
-        if (o.warm_restart && kh[s].status == ST_CONVERGED && rnorm[s] > 0.0) {
-          warm.push_back(s);
-          wti.push_back(ti);
-          wsig.push_back(rn_prev[s] / rnorm[s]);
-        } else {
-          cold.push_back(s);
-          cti.push_back(ti);
-        }
+        restart.push_back(s);
+        rti.push_back(std::min(0.5, std::max(o.inner_tol, 0.5 * tol[s] / rel)));
       }
     }
-    start_inner(cold, cti);
-    start_inner_warm(warm, wti, wsig);
+    start_inner(restart, rti);
     running = still;
-    running.insert(running.end(), cold.begin(), cold.end());
-    running.insert(running.end(), warm.begin(), warm.end());
+    running.insert(running.end(), restart.begin(), restart.end());
     std::sort(running.begin(), running.end());
   }
   CSEM_CUDA_TRY(cudaStreamSynchronize(st));

@@ -11,9 +11,9 @@ struct MixedOptions {
   int max_inner_total = 3000;
   int max_outer = 30;
   int preco = 1;            // 1 LU-SGS, 3 A-phi
-  double inner_tol = 1e-4;  // relative reduction asked of one inner solve
+  double inner_tol = 0.1;   // relative reduction asked of one inner solve
   int check_every = 4;      // inner iterations between host status reads
-  bool warm_restart = false;  // continue the Krylov recursion across defect corrections
+  bool autotune = false;    // time the LU-SGS sweep variants on the batch, keep the fastest
 };
 
 struct MixedResult {
@@ -33,7 +33,7 @@ class MixedBatch {
   int nblk;
   Ops<F64> o64;
   Ops<F32> o32;
-  DevBuf x64, b64, r64, w64, vec32, ks, sc64, sc32, dots, partial, list, rn, sig, srcbuf, chbuf, recbuf, outbuf;
+  DevBuf x64, b64, r64, w64, vec32, ks, sc64, sc32, dots, partial, list, rn, srcbuf, chbuf, recbuf, outbuf;
   float2* V(int i) { return vec32.as<float2>() + (size_t)i * nsys * n; }
   // b64 := injected sources (src [nsys][3], iom [nsys] on the host)
   void inject(const float* src, const double* iom, int nch, const int* ch);
@@ -42,12 +42,12 @@ class MixedBatch {
   // out [nsys][nch][nrec] complex128 from x64
   void extract(int nch, const int* ch, int nrec, const float* rec, double* out_host);
   double inner_seconds = 0, outer_seconds = 0;
+  int tuned_vw = 0;  // sweep width chosen by autotune_lusgs (0: not tuned)
   long inner_launch_iters = 0;  // sum over launched iterations of active systems
  private:
   void inner_iteration(int nact, const int* dlist, int preco, int maxiter);
   void start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner);
-  void start_inner_warm(const std::vector<int>& g, const std::vector<double>& tol_inner,
-                        const std::vector<double>& sigma);
+  int autotune_lusgs(int nact, const int* dlist);  // returns the chosen points per thread
   void outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first);
 };
 

@@ -116,7 +116,7 @@ typedef struct csem_batch_opts {
   int preco;         /* 0 none, 1 LU-SGS, 2 inner GMRES (64 only), 3 A-phi */
   int niter;         /* the reference's niter */
   float tol;         /* the reference's tol; system s stops at tol/freq[s] in float (main.c:94) */
-  double inner_tol;  /* precision 32: relative reduction of one inner solve (<= 0: 1e-4) */
+  double inner_tol;  /* precision 32: relative reduction of one inner solve (<= 0: 0.1) */
   int check_every;   /* precision 32: inner iterations between status reads (<= 0: 4) */
   int max_outer;     /* precision 32: defect-correction cycles (<= 0: 30) */
   int nrestart, mp;  /* precision 64: GMRES(nrestart) and GMRES(mp) preconditioner */
@@ -160,10 +160,12 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     lockstep pipeline; 0: one launch per wavefront diagonal;
  *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
  *                     0 for the default (2 complex64, 1 complex128).
- * Solver option (changes iteration counts, not the stopping test):
- *   "mixed_warm_restart" 1: after each defect correction the complex64 inner BiCGStab
- *                     continues with the true residual in place of its own;
- *                     0 (default): it restarts from the new residual. */
+ *   "autotune"        1: the batched mixed-precision solve times the complex64 LU-SGS
+ *                     sweep variants (points per thread 1, 2, 4) on its first running
+ *                     systems and keeps the fastest for that batch; 0 (default): the
+ *                     fixed default. complex64 results may then differ in the last bits
+ *                     from run to run, so it is off by default.
+ */
 int csem_ctx_set_option(csem_ctx *c, const char *name, int value);
 
 /* ------------------------------------------------------------ timing

@@ -75,23 +75,21 @@ def test_mixed_batch_matches_fp64(gpu, small_case):
             assert relerr(r32["dcal"][s, c], r64["dcal"][s, c]) <= 1e-6, (s, c, relerr(r32["dcal"][s, c], r64["dcal"][s, c]))
 
 
-def test_warm_and_cold_restarts_agree(gpu, small_case):
-    """The inner complex64 BiCGStab either continues across defect corrections with the
-    true residual in place of its own (warm) or restarts (cold, the default); both must
-    reach the same stopping test and agree with each other."""
+def test_autotuned_batch_matches_fp64(gpu, small_case):
+    """With the LU-SGS autotuner on, the batch still converges to the complex128 answer."""
     cfg, G, ctx, p, src = small_case
     freqs, srcs = _systems(cfg, src)
     rec = cfg.acq.rec
-    out = {}
-    for warm in (1, 0):
-        ctx.set_option("mixed_warm_restart", warm)
-        out[warm] = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=32, preco=1, niter=400, tol=1e-8)
-    ctx.set_option("mixed_warm_restart", 0)
-    for warm in (1, 0):
-        assert all(s == "converged" for s in out[warm]["status"]), (warm, out[warm])
+    r64 = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=64, preco=1, niter=400, tol=1e-8)
+    ctx.set_option("autotune", 1)
+    try:
+        r32 = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=32, preco=1, niter=400, tol=1e-8)
+    finally:
+        ctx.set_option("autotune", 0)
+    assert all(s == "converged" for s in r32["status"]), r32
     for s in range(len(freqs)):
         for c in range(3):
-            assert relerr(out[1]["dcal"][s, c], out[0]["dcal"][s, c]) <= 1e-6
+            assert relerr(r32["dcal"][s, c], r64["dcal"][s, c]) <= 1e-6
 
 
 def test_mixed_batch_aphi(gpu, small_case):
