@@ -287,6 +287,19 @@ def run_ours(args):
     return result, cfg, freqs, systems
 
 
+def measured_traffic(kernel: str):
+    """DRAM bytes per system and application of an operator from its committed ncu
+    summary (the `traffic_bytes_per_system:` line), or None."""
+    f = {"lusgs32": "k_sweep_lusgs32_marlim_like_96.md", "stencil32": "k_fdfd32_marlim_like_96.md"}.get(kernel)
+    path = os.path.join(ROOT, "profiles", f) if f else None
+    if not path or not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_system:"):
+            return int(line.split(":")[1])
+    return None
+
+
 def roofline(res, peaks):
     """Dominant operator (largest summed device time) and its algorithmic HBM bytes."""
     lE = res["lE"]
@@ -305,9 +318,14 @@ def roofline(res, peaks):
     for k, (m, c, units) in cands.items():
         sys_per_app = units / c
         achieved = bytes_per_sys[k] * sys_per_app / (m / c / 1e3) / 1e9
+        tps = measured_traffic(k) if res["lE"] == 11064870 else None  # captured on this workload only
         out[k] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
                   "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback",
-                  "unit": "GB/s", "frac": round(achieved / hbm, 3), "traffic": None, "avg_ms": round(m / c, 4),
+                  "unit": "GB/s", "frac": round(achieved / hbm, 3),
+                  "traffic": round(tps * sys_per_app) if tps else None,
+                  "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 4-system capture, per "
+                                    "system, times the systems per application" if tps else None,
+                  "avg_ms": round(m / c, 4),
                   "applications": c, "systems_per_application": round(sys_per_app, 2),
                   "algorithmic_bytes_per_system": bytes_per_sys[k]}
     return dom, out

@@ -15,7 +15,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 HOST = os.path.join(PKG, "host")
-OUT = os.path.join(PKG, "_build")
+# CSEM_BUILD_DIR puts a build elsewhere (e.g. variants built with CSEM_NVCC_FLAGS)
+OUT = os.environ.get("CSEM_BUILD_DIR") or os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libcsem_gpu.so")
 DRIVER = os.path.join(OUT, "csem")
 REFABI = os.path.join(OUT, "libcsem_refabi.so")
@@ -56,7 +57,7 @@ def _run(cmd: list[str], verbose: bool) -> None:
 
 def _compile_cu(src: str, obj: str, verbose: bool, extra: list[str]) -> str:
     cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-           "-I", INCLUDE, "-c", src, "-o", obj, *extra]
+           "-I", INCLUDE, "-c", src, "-o", obj, *extra, *os.environ.get("CSEM_NVCC_FLAGS", "").split()]
     _run(cmd, verbose)
     return obj
 

@@ -34,6 +34,16 @@ namespace {
 constexpr int MAXROWS = 256;  // rows of one sweep handled by one CTA (a thread each)
 // resident CTAs per SM the register budget is sized for, by points per thread and step
 template <int VW> struct MinBlocks { static constexpr int value = VW >= 4 ? 1 : (VW == 2 ? 2 : 3); };
+// Register budget of the sweeps: by default from MinBlocks for a full 256-row CTA; a build
+// may set explicit caps per width (CSEM_SWEEP_MAXNREG1 / 2 / 4) instead.
+#if defined(CSEM_SWEEP_MAXNREG1) && defined(CSEM_SWEEP_MAXNREG2) && defined(CSEM_SWEEP_MAXNREG4)
+template <int VW> struct RegCap {
+  static constexpr int value = VW == 1 ? CSEM_SWEEP_MAXNREG1 : (VW == 2 ? CSEM_SWEEP_MAXNREG2 : CSEM_SWEEP_MAXNREG4);
+};
+#define CSEM_SWEEP_BOUNDS(VW) __launch_bounds__(MAXROWS) __maxnreg__(RegCap<VW>::value)
+#else
+#define CSEM_SWEEP_BOUNDS(VW) __launch_bounds__(MAXROWS, MinBlocks<VW>::value)
+#endif
 
 template <class P> struct View {
   typedef typename P::C C;
@@ -293,7 +303,7 @@ __device__ __forceinline__ void hand_over_finish(int nsteps)
 
 // Ex sweep: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
 template <class P, bool FWD, int VW>
-__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(SweepP<P> s)
+__global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_ex(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
@@ -390,7 +400,7 @@ __global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_ex(Swee
 // Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j) sweeps, march i in chunks
 // of VW. grid (lines, systems)
 template <class P, int COMP, bool FWD, int VW>
-__global__ void __launch_bounds__(MAXROWS, MinBlocks<VW>::value) k_sweep_eyz(SweepP<P> s)
+__global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_eyz(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
