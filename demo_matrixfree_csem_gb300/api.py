@@ -87,6 +87,8 @@ def lib(build_if_missing: bool = True):
         "csem_ctx_sync": (C.c_int, [C.c_void_p]),
         "csem_ctx_stream": (C.c_void_p, [C.c_void_p]),
         "csem_ctx_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+        "csem_batch_bytes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp]),
+        "csem_batch_capacity": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _ip]),
         "csem_fdfd_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_lusgs_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_aphi_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -233,6 +235,18 @@ class Ctx:
         _check(lib().csem_ctx_sizes(self.h, s))
         (self.lE, self.lEx, self.lEy, self.lEz, self.lv, self.n1, self.n2, self.n3, self.n3f, self.nb) = list(s)
         self.airbc, self.fvm = airbc, fvm
+
+    def batch_bytes(self, nsys: int, precision: int = 32, preco: int = 1) -> float:
+        """Device bytes a batched solve of nsys systems needs beyond the model."""
+        b = C.c_double(0)
+        _check(lib().csem_batch_bytes(self.h, precision, preco, nsys, C.byref(b)))
+        return b.value
+
+    def batch_capacity(self, budget_bytes: float, precision: int = 32, preco: int = 1) -> int:
+        """Largest number of systems one batched solve can hold within budget_bytes."""
+        n = C.c_int(0)
+        _check(lib().csem_batch_capacity(self.h, precision, preco, float(budget_bytes), C.byref(n)))
+        return n.value
 
     def set_option(self, name: str, value: int) -> None:
         """Kernel-schedule options, e.g. set_option("lusgs_pipelined", 0)."""

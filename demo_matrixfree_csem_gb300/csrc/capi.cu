@@ -1,4 +1,6 @@
 // extern "C" entry points of libcsem_gpu.so (declared in include/csem_gpu.h).
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -165,6 +167,52 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     configure(c, c->batch->o64);
     configure(c, c->batch->o32);
   }
+  return CSEM_OK;
+}
+
+// Device bytes a batch of nsys systems needs on this context (MixedBatch and its two
+// operator sets, or the complex128 solver), excluding the model itself and cuFFT's work
+// areas.
+static double batch_bytes(const Model* m, int precision, int preco, int nsys)
+{
+  const double lE = (double)m->lE, lv = (double)m->lv;
+  auto ops = [&](double cs) {
+    double b = 0;
+    if (m->airbc) {
+      const double capE = (double)m->nb * ((double)m->n1 * (m->n2 + 1) + (double)(m->n1 + 1) * m->n2 +
+                                           (double)(m->n1 + 1) * (m->n2 + 1));
+      b += cs * ((double)m->n1 * m->n2 + 3.0 * m->N1 * m->N2 + (double)(m->n1 + 1) * m->n2 +
+                 (double)m->n1 * (m->n2 + 1) + capE);
+    }
+    if (preco == PRE_APHI) b += 2.0 * cs * lv;
+    return b;
+  };
+  if (precision == 32) {
+    // x, b, r, w in complex128; 8 complex64 Krylov vectors; per-system scalars
+    return nsys * (4.0 * 16 * lE + 8.0 * 8 * lE + ops(16) + ops(8) + 4096.0);
+  }
+  // the complex128 solver runs one system at a time: 7 BiCGStab vectors or GMRES(m) bases
+  return 16.0 * lE * 40 + ops(16);
+}
+
+int csem_batch_bytes(csem_ctx* c, int precision, int preco, int nsys, double* bytes)
+{
+  if (!c || !bytes || nsys < 1 || (precision != 32 && precision != 64))
+    return csem_set_error(CSEM_EINVAL, "csem_batch_bytes: bad argument");
+  *bytes = batch_bytes(c->model, precision, preco, nsys);
+  return CSEM_OK;
+}
+
+int csem_batch_capacity(csem_ctx* c, int precision, int preco, double budget_bytes, int* nsys)
+{
+  if (!c || !nsys || (precision != 32 && precision != 64))
+    return csem_set_error(CSEM_EINVAL, "csem_batch_capacity: bad argument");
+  if (precision == 64) {
+    *nsys = budget_bytes >= batch_bytes(c->model, 64, preco, 1) ? 1 << 30 : 0;
+    return CSEM_OK;
+  }
+  const double one = batch_bytes(c->model, 32, preco, 1);
+  *nsys = one > 0 ? (int)std::min(1.0e9, std::floor(budget_bytes / one)) : 0;
   return CSEM_OK;
 }
 

@@ -51,8 +51,13 @@ __device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __r
 // plane). Its column's spacings stay in registers and its element offsets advance by one
 // plane stride per plane; the plane's spacings are uniform loads. H is evaluated exactly
 // as in h_at, so complex128 results keep their bits.
+// resident CTAs per SM the complex64 stencil's register budget is sized for (a build may
+// set CSEM_FDFD_MINB to try others)
+#ifndef CSEM_FDFD_MINB
+#define CSEM_FDFD_MINB 3
+#endif
 template <class P, int BY>
-__global__ void __launch_bounds__(32 * (BY + 1), P::exact ? 1 : 2)
+__global__ void __launch_bounds__(32 * (BY + 1), P::exact ? 1 : CSEM_FDFD_MINB)
 k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
        typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
        const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list)
@@ -233,7 +238,10 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
                  const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
                  cudaStream_t st)
 {
-  constexpr int BY = 8;
+#ifndef CSEM_FDFD_BY
+#define CSEM_FDFD_BY 8
+#endif
+  constexpr int BY = CSEM_FDFD_BY;  // output rows per CTA (a build may set others to try)
   dim3 blk(32, BY + 1);
   const int gx = (g.n1 + 1 + 30) / 31, gy = (g.n2 + 1 + BY - 1) / BY;
   const long base = (long)gx * gy * nsys;

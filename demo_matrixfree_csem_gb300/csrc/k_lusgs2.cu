@@ -31,18 +31,22 @@ namespace csem {
 
 namespace {
 
-constexpr int MAXROWS = 256;  // rows of one sweep handled by one CTA (a thread each)
+constexpr int MAXROWS = 512;   // rows of one sweep handled by one CTA (a thread each)
+constexpr int NB_ROWS = 256;   // up to this many rows the warps hand over through named barriers
 // resident CTAs per SM the register budget is sized for, by points per thread and step
-template <int VW> struct MinBlocks { static constexpr int value = VW >= 4 ? 1 : (VW == 2 ? 2 : 3); };
-// Register budget of the sweeps: by default from MinBlocks for a full 256-row CTA; a build
-// may set explicit caps per width (CSEM_SWEEP_MAXNREG1 / 2 / 4) instead.
+// (complex128 at one point per thread keeps 2, whose 128 registers avoid spilling)
+template <class P, int VW> struct MinBlocks {
+  static constexpr int value = VW >= 4 ? 1 : (VW == 2 ? 2 : (P::exact ? 2 : 3));
+};
+// Register budget of the sweeps: by default from MinBlocks for a full CTA; a build may set
+// explicit caps per width (CSEM_SWEEP_MAXNREG1 / 2 / 4) for CTAs of up to 256 rows instead.
 #if defined(CSEM_SWEEP_MAXNREG1) && defined(CSEM_SWEEP_MAXNREG2) && defined(CSEM_SWEEP_MAXNREG4)
 template <int VW> struct RegCap {
   static constexpr int value = VW == 1 ? CSEM_SWEEP_MAXNREG1 : (VW == 2 ? CSEM_SWEEP_MAXNREG2 : CSEM_SWEEP_MAXNREG4);
 };
-#define CSEM_SWEEP_BOUNDS(VW) __launch_bounds__(MAXROWS) __maxnreg__(RegCap<VW>::value)
+#define CSEM_SWEEP_BOUNDS(VW, MAXR) __launch_bounds__(MAXR) __maxnreg__(MAXR > NB_ROWS ? 128 : RegCap<VW>::value)
 #else
-#define CSEM_SWEEP_BOUNDS(VW) __launch_bounds__(MAXROWS, MinBlocks<VW>::value)
+#define CSEM_SWEEP_BOUNDS(VW, MAXR) __launch_bounds__(MAXR, MAXR > NB_ROWS ? 1 : MinBlocks<P, VW>::value)
 #endif
 
 template <class P> struct View {
@@ -254,60 +258,92 @@ template <class C> __device__ __forceinline__ C shfl_up(C v)
 __device__ __forceinline__ void nbar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
 __device__ __forceinline__ void nbar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
 
-// Value the row before this thread's row produced at the previous step: a shuffle from
-// the previous lane, or the hand-over slot for lane 0; the sweep's first row reads the
-// zero boundary.
-template <int VW, class C>
-__device__ __forceinline__ void neighbours(const C (&res)[VW], C (&nb)[VW], const C (*hand)[VW], int T)
-{
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// Hand-over state of one CTA. Up to 256 rows (8 warps): the one-slot buffer with the
+// pairwise named barriers described above. Larger CTAs (up to 16 warps; there are only
+// 16 named barriers) use a two-slot buffer and one CTA barrier per step instead.
+template <int VW, class C, bool NAMED> struct HandOff;
+
+template <int VW, class C> struct HandOff<VW, C, true> {
+  C slot[NB_ROWS / 32][VW];
+  // the value the row before this thread's row produced at the previous step: a shuffle
+  // from the previous lane, or the slot for lane 0; the first row reads the zero boundary
+  __device__ __forceinline__ void get(const C (&res)[VW], C (&nb)[VW], int T)
+  {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < VW; q++) nb[q] = shfl_up(res[q]);
-  if (w > 0 && T > 0) {
-    nbar_sync(1 + 2 * (w - 1));  // warp w-1 has written step T-1
+    for (int q = 0; q < VW; q++) nb[q] = shfl_up(res[q]);
+    if (w > 0 && T > 0) {
+      nbar_sync(1 + 2 * (w - 1));  // warp w-1 has written step T-1
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < VW; q++) nb[q] = slot[w - 1][q];
+      }
+      nbar_arrive(2 + 2 * (w - 1));  // the slot may be rewritten
+    } else if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < VW; q++) {
+        nb[q].x = 0;
+        nb[q].y = 0;
+      }
+    }
+  }
+  __device__ __forceinline__ void put(const C (&res)[VW], int T)
+  {
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (w + 1 >= nw) return;  // the last warp feeds nobody
+    if (T >= 1) nbar_sync(2 + 2 * w);  // warp w+1 has read step T-1
+    if ((threadIdx.x & 31) == 31) {
+#pragma unroll
+      for (int q = 0; q < VW; q++) slot[w][q] = res[q];
+    }
+    nbar_arrive(1 + 2 * w);
+  }
+  // completes the last generation of the "full" barriers after the step loop
+  __device__ __forceinline__ void finish(int nsteps)
+  {
+    const int w = threadIdx.x >> 5;
+    if (w > 0 && nsteps > 0) nbar_sync(1 + 2 * (w - 1));
+  }
+};
+
+template <int VW, class C> struct HandOff<VW, C, false> {
+  C slot[2][MAXROWS / 32][VW];
+  __device__ __forceinline__ void get(const C (&res)[VW], C (&nb)[VW], int T)
+  {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < VW; q++) nb[q] = shfl_up(res[q]);
     if (lane == 0) {
 #pragma unroll
-      for (int q = 0; q < VW; q++) nb[q] = hand[w - 1][q];
-    }
-    nbar_arrive(2 + 2 * (w - 1));  // the slot may be rewritten
-  } else if (lane == 0) {
-#pragma unroll
-    for (int q = 0; q < VW; q++) {
-      nb[q].x = 0;
-      nb[q].y = 0;
+      for (int q = 0; q < VW; q++) {
+        C v;
+        v.x = 0;
+        v.y = 0;
+        if (w > 0 && T > 0) v = slot[(T - 1) & 1][w - 1][q];
+        nb[q] = v;
+      }
     }
   }
-}
-
-template <int VW, class C>
-__device__ __forceinline__ void hand_over(const C (&res)[VW], C (*hand)[VW], int T)
-{
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (w + 1 >= nw) return;  // the last warp feeds nobody
-  if (T >= 1) nbar_sync(2 + 2 * w);  // warp w+1 has read step T-1
-  if ((threadIdx.x & 31) == 31) {
+  __device__ __forceinline__ void put(const C (&res)[VW], int T)
+  {
+    if ((threadIdx.x & 31) == 31) {
 #pragma unroll
-    for (int q = 0; q < VW; q++) hand[w][q] = res[q];
+      for (int q = 0; q < VW; q++) slot[T & 1][threadIdx.x >> 5][q] = res[q];
+    }
+    __syncthreads();
   }
-  nbar_arrive(1 + 2 * w);
-}
-
-// Completes the last generation of the "full" barriers after the step loop.
-__device__ __forceinline__ void hand_over_finish(int nsteps)
-{
-  const int w = threadIdx.x >> 5;
-  if (w > 0 && nsteps > 0) nbar_sync(1 + 2 * (w - 1));
-}
+  __device__ __forceinline__ void finish(int) {}
+};
 
 }  // namespace
 
 // Ex sweep: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
-template <class P, bool FWD, int VW>
-__global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_ex(SweepP<P> s)
+template <class P, bool FWD, int VW, int MAXR>
+__global__ void CSEM_SWEEP_BOUNDS(VW, MAXR) k_sweep_ex(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
-  __shared__ C hand[MAXROWS / 32][VW];
+  __shared__ HandOff<VW, C, (MAXR <= NB_ROWS)> hand;
   const int slot = blockIdx.y;
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
@@ -346,7 +382,7 @@ __global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_ex(SweepP<P> s)
   for (int q = 0; q < VW; q++) res[q] = z;
   for (int T = 0; T < M + R_ - 1; T++) {
     C nb[VW];
-    neighbours<VW, C>(res, nb, hand, T);
+    hand.get(res, nb, T);
     const int c = T - rr;
     if (rowok && c >= 0 && c < M) {
       const int j = FWD ? 1 + c : M - c;
@@ -392,19 +428,19 @@ __global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_ex(SweepP<P> s)
 #pragma unroll
       for (int q = 0; q < VW; q++) res[q] = z;
     }
-    hand_over<VW, C>(res, hand, T);
+    hand.put(res, T);
   }
-  hand_over_finish(M + R_ - 1);
+  hand.finish(M + R_ - 1);
 }
 
 // Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j) sweeps, march i in chunks
 // of VW. grid (lines, systems)
-template <class P, int COMP, bool FWD, int VW>
-__global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_eyz(SweepP<P> s)
+template <class P, int COMP, bool FWD, int VW, int MAXR>
+__global__ void CSEM_SWEEP_BOUNDS(VW, MAXR) k_sweep_eyz(SweepP<P> s)
 {
   typedef typename P::C C;
   typedef typename P::R R;
-  __shared__ C hand[MAXROWS / 32][VW];
+  __shared__ HandOff<VW, C, (MAXR <= NB_ROWS)> hand;
   const int slot = blockIdx.y;
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<P>& g = s.g;
@@ -466,7 +502,7 @@ __global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_eyz(SweepP<P> s)
   for (int q = 0; q < VW; q++) res[q] = z;
   for (int T = 0; T < NC + R_ - 1; T++) {
     C nb[VW];
-    neighbours<VW, C>(res, nb, hand, T);
+    hand.get(res, nb, T);
     const int c = T - rr;
     if (rowok && c >= 0 && c < NC) {
       C prev = c > 0 ? res[VW - 1] : z;  // own row at the previous march position
@@ -529,9 +565,9 @@ __global__ void CSEM_SWEEP_BOUNDS(VW) k_sweep_eyz(SweepP<P> s)
 #pragma unroll
       for (int q = 0; q < VW; q++) res[q] = z;
     }
-    hand_over<VW, C>(res, hand, T);
+    hand.put(res, T);
   }
-  hand_over_finish(NC + R_ - 1);
+  hand.finish(NC + R_ - 1);
 }
 
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
@@ -540,7 +576,7 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
   return rows >= 1 && rows <= MAXROWS && n1 >= 2 && n2 >= 2;
 }
 
-template <class P, int VW>
+template <class P, int VW, int MAXR>
 static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st)
 {
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
@@ -548,28 +584,35 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
   const int threads = (rows + 31) / 32 * 32;
   if (comp == 0) {
     dim3 grd((n1 + VW - 1) / VW, nslot);
-    if (fwd) count_launch(), k_sweep_ex<P, true, VW><<<grd, threads, 0, st>>>(s);
-    else count_launch(), k_sweep_ex<P, false, VW><<<grd, threads, 0, st>>>(s);
+    if (fwd) count_launch(), k_sweep_ex<P, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    else count_launch(), k_sweep_ex<P, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
   } else if (comp == 1) {
     dim3 grd(n2, nslot);
-    if (fwd) count_launch(), k_sweep_eyz<P, 1, true, VW><<<grd, threads, 0, st>>>(s);
-    else count_launch(), k_sweep_eyz<P, 1, false, VW><<<grd, threads, 0, st>>>(s);
+    if (fwd) count_launch(), k_sweep_eyz<P, 1, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    else count_launch(), k_sweep_eyz<P, 1, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
   } else {
     dim3 grd(nK, nslot);
-    if (fwd) count_launch(), k_sweep_eyz<P, 2, true, VW><<<grd, threads, 0, st>>>(s);
-    else count_launch(), k_sweep_eyz<P, 2, false, VW><<<grd, threads, 0, st>>>(s);
+    if (fwd) count_launch(), k_sweep_eyz<P, 2, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    else count_launch(), k_sweep_eyz<P, 2, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
   }
 }
 
 // vw: points per thread and step (1, 2 or 4; other values select the default, the
-// fastest measured on a 200x140x140 grid: 2 for complex64, 1 for complex128)
+// fastest measured on a 200x140x140 grid: 2 for complex64, 1 for complex128). Sweeps of
+// more than 256 rows run 1 or 2 points per thread in CTAs of up to 512 threads.
 template <class P>
 void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw)
 {
   if (vw != 1 && vw != 2 && vw != 4) vw = P::exact ? 1 : 2;
-  if (vw == 1) launch_vw<P, 1>(s, comp, fwd, nslot, st);
-  else if (vw == 2) launch_vw<P, 2>(s, comp, fwd, nslot, st);
-  else launch_vw<P, 4>(s, comp, fwd, nslot, st);
+  const int rows = comp == 2 ? s.g.n2 - 1 : s.nK - 1;
+  if (rows > NB_ROWS) {
+    if (vw == 1) launch_vw<P, 1, MAXROWS>(s, comp, fwd, nslot, st);
+    else launch_vw<P, 2, MAXROWS>(s, comp, fwd, nslot, st);
+    return;
+  }
+  if (vw == 1) launch_vw<P, 1, NB_ROWS>(s, comp, fwd, nslot, st);
+  else if (vw == 2) launch_vw<P, 2, NB_ROWS>(s, comp, fwd, nslot, st);
+  else launch_vw<P, 4, NB_ROWS>(s, comp, fwd, nslot, st);
 }
 
 template void launch_sweep_pipelined<F64>(const SweepP<F64>&, int, bool, int, cudaStream_t, int);

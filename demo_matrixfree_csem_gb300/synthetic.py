@@ -182,6 +182,54 @@ def marlim_like(seed: int = 0, freqs=(0.125, 0.25, 0.5, 0.75, 1.0, 1.25), nsrc: 
     return Config(model, Acquisition(src, rec), params, name="marlim_like")
 
 
+def large_420(seed: int = 2, freqs=(0.125, 0.25, 0.5, 0.75, 1.0, 1.25), nsrc: int = 32) -> Config:
+    """Large memory-bound batch: 400x400x200 core cells of 50 m padded by nb=10 to
+    420x420x220 (about 116M complex edge unknowns per system), a seeded layered
+    anisotropic model built as marlim_like (seafloor 1500 m, 30 layers of 100 m,
+    rho33 = 1.5 rho11) with 8 seeded resistors; 32 Ex sources along y=0, 6 frequencies:
+    192 systems, solved in waves that fit device memory."""
+    rng = np.random.default_rng(seed)
+    x1 = np.arange(-10000, 10001, 50, dtype=np.float32)
+    x2 = x1.copy()
+    x3 = np.arange(0, 10001, 50, dtype=np.float32)
+    xc, yc, zc = _centres(x1), _centres(x2), _centres(x3)
+    nz, ny, nx = len(zc), len(yc), len(xc)
+    seafloor = 1500.0
+    layer_rho = np.exp(rng.uniform(np.log(0.5), np.log(5.0), size=30))
+    rz = np.full(nz, 0.3)
+    for L in range(30):
+        rz[(zc >= seafloor + 100 * L) & (zc < seafloor + 100 * (L + 1))] = layer_rho[L]
+    rz[zc >= seafloor + 3000] = layer_rho[-1]
+    rho11 = np.broadcast_to(rz[:, None, None], (nz, ny, nx)).astype(np.float32).copy()
+    rho33 = np.broadcast_to(np.where(zc >= seafloor, 1.5 * rz, rz)[:, None, None], (nz, ny, nx)).astype(np.float32).copy()
+    for _ in range(8):
+        r = rng.uniform(20, 100)
+        ax, ay, az = rng.uniform(500, 3000), rng.uniform(500, 3000), rng.uniform(50, 200)
+        cx, cy = rng.uniform(-7000, 7000), rng.uniform(-7000, 7000)
+        cz = rng.uniform(seafloor + 400, seafloor + 2600)
+        kz = np.nonzero(np.abs(zc - cz) <= az)[0]
+        jy = np.nonzero(np.abs(yc - cy) <= ay)[0]
+        ix = np.nonzero(np.abs(xc - cx) <= ax)[0]
+        if not (len(kz) and len(jy) and len(ix)):
+            continue
+        Z, Y, X = np.meshgrid(zc[kz], yc[jy], xc[ix], indexing="ij")
+        inside = ((X - cx) / ax) ** 2 + ((Y - cy) / ay) ** 2 + ((Z - cz) / az) ** 2 <= 1.0
+        sub = np.ix_(kz, jy, ix)
+        rho11[sub] = np.where(inside, r, rho11[sub])
+        rho33[sub] = np.where(inside, r, rho33[sub])
+    model = Model(x1, x2, x3, rho11, rho11.copy(), rho33, name="large_420")
+    sx = -7750.0 + 500.0 * np.arange(nsrc)
+    src = np.stack([sx, np.zeros(nsrc), np.full(nsrc, seafloor - 50.0), np.zeros(nsrc),
+                    np.zeros(nsrc)], axis=1).astype(np.float32)
+    rx = np.arange(-9800, 9801, 200, dtype=np.float64)
+    rec = np.stack([rx, np.zeros_like(rx), np.full_like(rx, seafloor), np.zeros_like(rx),
+                    np.zeros_like(rx)], axis=1).astype(np.float32)
+    params = dict(airbc=1, nb=10, lextend="40e3", preco=1, algopt=1, tol="1e-8", niter=1000,
+                  fvm=0, chsrc="Ex", chrec="Ex,Ey,Ez",
+                  freqs=",".join(str(f) for f in freqs))
+    return Config(model, Acquisition(src, rec), params, name="large_420")
+
+
 def random_small(seed: int, nx=12, ny=10, nz=9, airbc=0, nb=3, aniso=True, stretch=True,
                  freqs=(0.5, 1.0), **extra) -> Config:
     """Small random model: random (optionally stretched) node spacings, random
@@ -226,11 +274,11 @@ def random_small(seed: int, nx=12, ny=10, nz=9, airbc=0, nb=3, aniso=True, stret
 
 
 WORKLOADS = {"marlim_like_96": lambda: marlim_like(seed=0), "layered_120": layered_120,
-             "vti_block_120": vti_block_120}
+             "vti_block_120": vti_block_120, "large_420_192": lambda: large_420(seed=2)}
 
 
 def workload(name: str) -> Config:
-    """A named benchmark workload (marlim_like_96, layered_120, vti_block_120)."""
+    """A named benchmark workload (marlim_like_96, layered_120, vti_block_120, large_420_192)."""
     if name not in WORKLOADS:
         raise ValueError(f"unknown workload {name}; known: {', '.join(WORKLOADS)}")
     return WORKLOADS[name]()

@@ -126,6 +126,15 @@ int csem_solve_batch_host(csem_ctx *c, int nsys, const float *freq, const float 
                           const csem_batch_opts *opt, double *dcal, int *iters, int *outer, int *status,
                           double *relres);
 
+/* Capacity planning for large sets of systems (no counterpart in the reference, which
+ * solves one system at a time). csem_batch_bytes: device bytes csem_solve_batch_host
+ * needs for nsys systems with this precision and preconditioner, beyond the model and
+ * cuFFT's work areas. csem_batch_capacity: the largest nsys whose batch fits in
+ * budget_bytes (precision 64 solves one system at a time: any count if one fits, else 0).
+ * Callers with more systems solve them in waves of that size. */
+int csem_batch_bytes(csem_ctx *c, int precision, int preco, int nsys, double *bytes);
+int csem_batch_capacity(csem_ctx *c, int precision, int preco, double budget_bytes, int *nsys);
+
 /* ------------------------------------------------------------ device-pointer entry points
  * For callers that keep vectors in GPU memory. nsys systems are stored back to back
  * (stride lE); iom is a host array of nsys (re, im) pairs. prec: 64 = complex128,

@@ -1,21 +1,22 @@
-"""Receiver fixtures of the layered 120^3 workload computed by the reference itself.
+"""Receiver fixtures of the 120^3 workloads computed by the reference itself.
 
-The reference (built from its sources by oracle/build_ref.sh) solves the layered
-workload of demo_matrixfree_csem_gb300.synthetic.layered_120 - 100^3 core cells of
-100 m, nb=10 padding to 120^3, airbc=1, one Ex dipole at (0,0,950), 101 seafloor
-receivers, BiCGStab + LU-SGS to tol=1e-8/f - one frequency per process, and this
+The reference (built from its sources by oracle/build_ref.sh) solves a workload of
+demo_matrixfree_csem_gb300.synthetic - layered_120 (100^3 core cells of 100 m, nb=10
+padding to 120^3, airbc=1, one Ex dipole at (0,0,950), 101 seafloor receivers) or
+vti_block_120 (the same grid, rho33 = 2 rho11, a 50 ohm-m 2 x 2 x 0.1 km block at
+2050 m) - with BiCGStab + LU-SGS to tol=1e-8/f, one frequency per process, and this
 script stores for each frequency:
   * the receivers in complex128 (the value extract_emf computes before its complex64
     store; the oracle's extraction is bit-identical to it), channels Ex, Ey, Ez;
   * the complex64 values the reference stores in dcal_fd;
   * the relative-residual history the reference prints (iterate_fbicgstab.txt) and the
     iteration count.
-Output: tests/golden/layered_120/reference_receivers.npz (a few tens of KB).
+Output: tests/golden/<workload>/reference_receivers.npz (a few tens of KB).
 
 FFTW is replaced by the self-written DFT of oracle/fft2d.c (see oracle/ref_stubs), so
 the airwave part of these numbers carries that transform's rounding.
 
-    python tests/golden/make_layered_reference.py          # all frequencies, in parallel
+    python tests/golden/make_reference_receivers.py [layered_120|vti_block_120]
 """
 from __future__ import annotations
 
@@ -30,14 +31,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-OUT = os.path.join(HERE, "layered_120", "reference_receivers.npz")
+def out_path(workload: str) -> str:
+    return os.path.join(HERE, workload, "reference_receivers.npz")
 
 
-def one(ifreq: int, work: str) -> None:
+def one(workload: str, ifreq: int, work: str) -> None:
     from demo_matrixfree_csem_gb300 import synthetic
     from oracle import Ref
     from oracle.pyoracle import Oracle
-    cfg = synthetic.layered_120()
+    cfg = synthetic.workload(workload)
     synthetic.write_config(cfg, work)
     os.chdir(work)
     R = Ref(cfg.args(work))
@@ -55,9 +57,11 @@ def one(ifreq: int, work: str) -> None:
 
 
 def main() -> None:
-    if len(sys.argv) == 3:
-        one(int(sys.argv[1]), sys.argv[2])
+    if len(sys.argv) == 4:
+        one(sys.argv[1], int(sys.argv[2]), sys.argv[3])
         return
+    workload = sys.argv[1] if len(sys.argv) > 1 else "layered_120"
+    OUT = out_path(workload)
     from oracle import build_ref, ref_available
     if not ref_available():
         sys.exit("reference sources not found")
@@ -67,7 +71,7 @@ def main() -> None:
     for w in works:
         os.makedirs(w)
     with cf.ThreadPoolExecutor(3) as ex:
-        list(ex.map(lambda i: subprocess.run([sys.executable, __file__, str(i), works[i]], check=True,
+        list(ex.map(lambda i: subprocess.run([sys.executable, __file__, workload, str(i), works[i]], check=True,
                                              stdout=subprocess.DEVNULL), range(3)))
     parts = [np.load(os.path.join(works[i], f"f{i}.npz")) for i in range(3)]
     os.makedirs(os.path.dirname(OUT), exist_ok=True)

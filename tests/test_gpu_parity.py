@@ -132,6 +132,28 @@ def test_larger_grid_bit_exact(gpu, tmp_path, airbc, fvm):
 
 
 @pytest.mark.parametrize("airbc", [0, 1])
+def test_tall_grid_lusgs_bit_exact(gpu, tmp_path, airbc):
+    """More than 256 rows in the Ez sweep (n2 - 1 > 256): CTAs of up to 512 threads that
+    hand over through a CTA barrier instead of the named-barrier pairs."""
+    cfg = synthetic.random_small(61 + airbc, nx=12, ny=290, nz=9, nb=4, airbc=airbc, n1fft=32, n2fft=512)
+    synthetic.write_config(cfg, str(tmp_path))
+    p = {k: str(v) for k, v in cfg.params.items()}
+    G = product_grid(str(tmp_path), p)
+    ctx = cs.Ctx(G, airbc, 0)
+    assert ctx.n2 - 1 > 256
+    O = oracle_for(G, p)
+    O.set_freq(0.5)
+    iom = cs.iom_of(0.5)
+    x = probe(ctx.lE, 8)
+    mo = O.lusgs(x)
+    for vw in (1, 2):
+        ctx.set_option("lusgs_vw", vw)
+        assert np.array_equal(ctx.lusgs_apply(iom, x), mo), vw
+        assert relerr(ctx.lusgs_apply(iom, x, c64=True), mo) <= 2e-5, vw
+    ctx.set_option("lusgs_vw", 0)
+
+
+@pytest.mark.parametrize("airbc", [0, 1])
 def test_aphi_larger_grid_bit_exact(gpu, tmp_path, airbc):
     cfg = synthetic.random_small(31 + airbc, nx=33, ny=21, nz=17, nb=3, airbc=airbc, n1fft=32, n2fft=32, preco=3)
     synthetic.write_config(cfg, str(tmp_path))
