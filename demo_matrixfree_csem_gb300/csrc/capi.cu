@@ -27,6 +27,7 @@ struct csem_ctx {
   bool lusgs_pipelined = true;
   int lusgs_vw = 0;
   bool autotune = false;
+  bool graphs = true;
 };
 
 // the context's kernel-schedule options on one operator set
@@ -157,6 +158,8 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     c->lusgs_vw = value;
   } else if (!strcmp(name, "autotune")) {
     c->autotune = value != 0;
+  } else if (!strcmp(name, "graphs")) {
+    c->graphs = value != 0;
   } else {
     return csem_set_error(CSEM_EINVAL, "unknown option %s", name);
   }
@@ -463,8 +466,10 @@ int csem_solve_batch_host(csem_ctx* c, int nsys, const float* freq, const float*
     return csem_set_error(CSEM_EINVAL, "precision must be 32 or 64");
   if (opt->precision == 32 && !(opt->preco == 1 || opt->preco == 3))
     return csem_set_error(CSEM_EINVAL, "the mixed-precision solver takes preco 1 (LU-SGS) or 3 (A-phi)");
-  if (opt->precision == 32 && opt->algopt != 1)
-    return csem_set_error(CSEM_EINVAL, "the mixed-precision solver runs BiCGStab (algopt=1)");
+  if (opt->precision == 32 && opt->algopt != 1 && opt->algopt != 2)
+    return csem_set_error(CSEM_EINVAL, "algopt must be 1 (BiCGStab) or 2 (GMRES)");
+  if (opt->precision == 32 && opt->algopt == 2 && (opt->nrestart < 1 || opt->nrestart > 64))
+    return csem_set_error(CSEM_EINVAL, "nrestart must be in 1..64");
   if (nchsrc < 1 || nchsrc > 8) return csem_set_error(CSEM_EINVAL, "1..8 source channels");
   API_BEGIN
   std::vector<double> iom(2 * nsys), tol(nsys);
@@ -486,6 +491,9 @@ int csem_solve_batch_host(csem_ctx* c, int nsys, const float* freq, const float*
     mo.inner_tol = opt->inner_tol > 0 ? opt->inner_tol : 0.1;
     mo.check_every = opt->check_every > 0 ? opt->check_every : 4;
     mo.autotune = c->autotune;
+    mo.algopt = opt->algopt;
+    mo.graphs = c->graphs;
+    mo.nrestart = opt->nrestart;
     std::vector<MixedResult> res;
     B->solve(iom.data(), tol.data(), mo, res);
     B->extract(nchrec, chrec, nrec, rec, dcal);

@@ -13,9 +13,11 @@
 // systems still iterating, so a converged system costs nothing once the host has seen
 // its status (read every `check_every` inner iterations).
 #include <algorithm>
+#include <complex>
 #include <cmath>
 #include <cstring>
 #include "solve_mixed.h"
+#include "../../include/csem_gpu.h"
 
 namespace csem {
 
@@ -67,6 +69,61 @@ MixedBatch::MixedBatch(Model* m_, int nsys_, cudaStream_t st_)
   partial.alloc(sizeof(double2) * (size_t)nblk * nsys);
   list.alloc(sizeof(int) * nsys);
   rn.alloc(sizeof(double) * nsys);
+}
+
+MixedBatch::~MixedBatch()
+{
+  for (auto& kv : graphs_)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+}
+
+// The iterations between two status reads are the same launch sequence every time for a
+// given number of running systems (their indices live in the device list the kernels
+// read), so from the second occurrence on they are captured once and replayed as a CUDA
+// graph. The first occurrence runs directly, which also creates everything created on
+// first use (FFT plans, A-phi work arrays) before any capture. Per-operator profiling
+// records events per application, so it keeps the direct launches.
+void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
+{
+  const int* dl = list.as<int>();
+  auto direct = [&]() {
+    for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
+  };
+  if (!o.graphs || prof_on()) {
+    direct();
+    return;
+  }
+  Graph& g = graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter)];
+  if (g.failed || g.seen++ == 0) {
+    direct();
+    return;
+  }
+  if (!g.exec) {
+    cudaGraph_t graph = nullptr;
+    const long long l0 = csem_launch_count();
+    CSEM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
+    } catch (...) {
+      cudaStreamEndCapture(st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    g.launches = (int)(csem_launch_count() - l0);
+    count_launch(-g.launches);  // captured, not launched yet
+    if (e != cudaSuccess || !graph || cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      (void)cudaGetLastError();
+      g.exec = nullptr;
+      g.failed = true;
+      direct();
+      return;
+    }
+    cudaGraphDestroy(graph);
+  }
+  CSEM_CUDA_TRY(cudaGraphLaunch(g.exec, st));
+  count_launch(g.launches);
 }
 
 void MixedBatch::inject(const float* src, const double* iom, int nch, const int* ch)
@@ -137,14 +194,14 @@ void MixedBatch::start_inner(const std::vector<int>& g, const std::vector<double
   CSEM_CUDA_TRY(cudaGetLastError());
 }
 
-void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first)
+void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first, const float2* d)
 {
   const int ng = (int)g.size();
   CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, g.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, st));
   const int* dl = list.as<int>();
   dim3 grd((unsigned)((n + 255) / 256), ng);
   if (!first) {
-    count_launch(), k_outer_accum<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), x64.as<double2>(), V(7));
+    count_launch(), k_outer_accum<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), x64.as<double2>(), d ? d : V(7));
     o64.apply_A(x64.as<double2>(), w64.as<double2>(), ng, dl, sc64.as<SysScal<F64>>());
     launch_vec<F64>(VEC_SUB, n, ng, dl, nullptr, b64.as<double2>(), w64.as<double2>(), r64.as<double2>(), nullptr,
                     nullptr, st);
@@ -226,6 +283,11 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
     running.push_back(q);
     ti.push_back(std::min(0.5, std::max(o.inner_tol, 0.5 * tol[q])));
   }
+  if (o.algopt == 2) {
+    solve_gmres(bn, tol, o, res, rnorm, running);
+    CSEM_CUDA_TRY(cudaStreamSynchronize(st));
+    return;
+  }
   if (o.autotune && o.preco != PRE_APHI && !running.empty()) {
     CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, running.data(), sizeof(int) * running.size(), cudaMemcpyHostToDevice, st));
     tuned_vw = autotune_lusgs((int)running.size(), list.as<int>());
@@ -235,10 +297,8 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
   inner_launch_iters = 0;
   while (!running.empty()) {
     CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, running.data(), sizeof(int) * running.size(), cudaMemcpyHostToDevice, st));
-    for (int q = 0; q < o.check_every; q++) {
-      inner_iteration((int)running.size(), list.as<int>(), o.preco, o.niter);
-      inner_launch_iters += (long)running.size();
-    }
+    inner_iterations((int)running.size(), o);
+    inner_launch_iters += (long)running.size() * o.check_every;
     CSEM_CUDA_TRY(cudaGetLastError());
     CSEM_CUDA_TRY(cudaMemcpyAsync(kh.data(), ks.p, sizeof(KrylovScalars) * nsys, cudaMemcpyDeviceToHost, st));
     CSEM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -267,6 +327,204 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
     std::sort(running.begin(), running.end());
   }
   CSEM_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// ------------------------------------------------------------------ flexible GMRES inner
+// The same defect correction with a complex64 flexible GMRES(m) as the inner solver, the
+// structure of fgmres (solver.c:403-512): z_j = M v_j, w = A z_j, modified Gram-Schmidt
+// against v_0..v_j, Givens rotations of the Hessenberg column, restart after m steps.
+// Vectors, preconditioner, operator and dot products run batched on the device over the
+// systems still iterating; the (m+1) x m Hessenberg algebra of every system runs in
+// complex128 on the host (one read of the batched dot products per Gram-Schmidt step).
+// A system leaves the step loop of a cycle when its estimated residual reaches the inner
+// reduction.
+namespace {
+typedef std::complex<double> zc;
+inline zc Z(double2 v) { return zc(v.x, v.y); }
+inline double2 D2(zc v) { return make_double2(v.real(), v.imag()); }
+}  // namespace
+
+std::vector<double2> MixedBatch::batch_dot(const float2* a, const float2* b, int ng, const int* dl)
+{
+  double2* Dd = dots.as<double2>();
+  launch_dot<F32>(a, b, n, n, ng, dl, partial.as<double2>(), nblk, Dd, st);
+  std::vector<double2> h(ng);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(h.data(), Dd, sizeof(double2) * ng, cudaMemcpyDeviceToHost, st));
+  CSEM_CUDA_TRY(cudaStreamSynchronize(st));
+  return h;
+}
+
+void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double>& tol_inner, const MixedOptions& o,
+                             std::vector<int>& iters)
+{
+  const int m = std::max(1, o.nrestart);
+  const size_t N = (size_t)nsys * n;
+  float2* base = gm.as<float2>();
+  auto GV = [&](int i) { return base + (size_t)i * N; };
+  auto GZ = [&](int i) { return base + (size_t)(m + 1 + i) * N; };
+  float2* GW = base + (size_t)(2 * m + 1) * N;
+  float2* GD = base + (size_t)(2 * m + 2) * N;
+  float2* GR0 = base + (size_t)(2 * m + 3) * N;
+  const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
+  double2* cf = gcoef.as<double2>();
+  auto M = [&](const float2* in, float2* out, int ng, const int* dl) {
+    if (o.preco == PRE_APHI) o32.apply_aphi(in, out, ng, dl, sc);
+    else o32.apply_lusgs(in, out, ng, dl, sc);
+  };
+  // r0 = r64 / |r64|, d = 0 (k_start_inner writes r, r0, p, d: here r0 twice and d)
+  {
+    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, g.data(), sizeof(int) * g.size(), cudaMemcpyHostToDevice, st));
+    dim3 grd((unsigned)((n + 255) / 256), (unsigned)g.size());
+    count_launch(), k_start_inner<<<grd, 256, 0, st>>>(n, list.as<int>(), rn.as<double>(), r64.as<double2>(), GR0, GR0,
+                                                       GW, GD);
+  }
+  const int ns = (int)g.size();
+  std::vector<double> beta0(ns, 1.0);
+  std::vector<char> done(ns, 0);
+  iters.assign(ns, 0);
+  std::vector<int> lists(nsys);
+  for (int cycle = 0;; cycle++) {
+    std::vector<int> act;  // positions in g of systems still solving
+    for (int q = 0; q < ns; q++)
+      if (!done[q] && iters[q] < o.niter) act.push_back(q);
+    if (act.empty()) break;
+    int na = (int)act.size();
+    std::vector<int> sl(na);
+    for (int a = 0; a < na; a++) sl[a] = g[act[a]];
+    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, sl.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st));
+    const int* dl = list.as<int>();
+    // r = r0 - A d  (d = 0 on the first cycle)
+    if (cycle == 0) {
+      CSEM_CUDA_TRY(cudaMemcpyAsync(GW, GR0, sizeof(float2) * N, cudaMemcpyDeviceToDevice, st));
+    } else {
+      o32.apply_A(GD, GV(0), na, dl, sc);
+      launch_vec<F32>(VEC_SUB, n, na, dl, nullptr, GR0, GV(0), GW, nullptr, nullptr, st);
+    }
+    std::vector<double2> bb = batch_dot(GW, GW, na, dl);
+    std::vector<double> beta(na);
+    std::vector<double2> cdiv(na);
+    for (int a = 0; a < na; a++) {
+      beta[a] = std::sqrt(bb[a].x);
+      if (cycle == 0) beta0[act[a]] = beta[a] > 0 ? beta[a] : 1.0;
+      cdiv[a] = make_double2(beta[a] > 0 ? beta[a] : 1.0, 0.0);
+    }
+    CSEM_CUDA_TRY(cudaMemcpyAsync(cf, cdiv.data(), sizeof(double2) * na, cudaMemcpyHostToDevice, st));
+    launch_cdivv<F32>(n, na, dl, cf, 1, 1, GW, GV(0), st);
+    // per-system Hessenberg (column j in H[j][0..j+1]), Givens and right-hand side
+    std::vector<std::vector<zc>> H(na, std::vector<zc>((size_t)m * (m + 1))), gg(na, std::vector<zc>(m + 1));
+    std::vector<std::vector<zc>> cs(na, std::vector<zc>(m));
+    std::vector<std::vector<double>> sn(na, std::vector<double>(m));
+    std::vector<int> steps(na, 0);
+    std::vector<char> stop(na, 0);
+    for (int a = 0; a < na; a++) gg[a][0] = zc(beta[a], 0.0);
+    for (int j = 0; j < m; j++) {
+      std::vector<int> live;  // positions in act of systems stepping
+      for (int a = 0; a < na; a++)
+        if (!stop[a]) live.push_back(a);
+      if (live.empty()) break;
+      const int nl = (int)live.size();
+      std::vector<int> ll(nl);
+      for (int b = 0; b < nl; b++) ll[b] = sl[live[b]];
+      CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, ll.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, st));
+      M(GV(j), GZ(j), nl, dl);
+      o32.apply_A(GZ(j), GW, nl, dl, sc);
+      for (int i = 0; i <= j; i++) {
+        std::vector<double2> h = batch_dot(GW, GV(i), nl, dl);
+        for (int b = 0; b < nl; b++) H[live[b]][(size_t)j * (m + 1) + i] = Z(h[b]);
+        CSEM_CUDA_TRY(cudaMemcpyAsync(cf, h.data(), sizeof(double2) * nl, cudaMemcpyHostToDevice, st));
+        launch_axpy<F32>(n, nl, dl, cf, 1, 1, GV(i), GW, st);
+      }
+      std::vector<double2> hn = batch_dot(GW, GW, nl, dl);
+      std::vector<double2> dv(nl);
+      for (int b = 0; b < nl; b++) {
+        const double hv = std::sqrt(hn[b].x);
+        H[live[b]][(size_t)j * (m + 1) + j + 1] = zc(hv, 0.0);
+        dv[b] = make_double2(hv > 0 ? hv : 1.0, 0.0);
+      }
+      CSEM_CUDA_TRY(cudaMemcpyAsync(cf, dv.data(), sizeof(double2) * nl, cudaMemcpyHostToDevice, st));
+      launch_cdivv<F32>(n, nl, dl, cf, 1, 1, GW, GV(j + 1), st);
+      for (int b = 0; b < nl; b++) {
+        const int a = live[b];
+        zc* col = &H[a][(size_t)j * (m + 1)];
+        for (int i = 0; i < j; i++) {  // earlier rotations
+          const zc t = std::conj(cs[a][i]) * col[i] + sn[a][i] * col[i + 1];
+          col[i + 1] = -sn[a][i] * col[i] + cs[a][i] * col[i + 1];
+          col[i] = t;
+        }
+        const double tmp = std::sqrt(std::norm(col[j]) + std::norm(col[j + 1]));
+        if (tmp == 0.0) {
+          stop[a] = 1;
+          continue;
+        }
+        sn[a][j] = col[j + 1].real() / tmp;
+        cs[a][j] = col[j] / tmp;
+        gg[a][j + 1] = -sn[a][j] * gg[a][j];
+        gg[a][j] = std::conj(cs[a][j]) * gg[a][j];
+        col[j] = std::conj(cs[a][j]) * col[j] + sn[a][j] * col[j + 1];
+        steps[a] = j + 1;
+        iters[act[a]] += 1;
+        const double rel = std::abs(gg[a][j + 1]) / beta0[act[a]];
+        if (rel < tol_inner[act[a]] || !(hn[b].x > 0.0)) {
+          stop[a] = 1;
+          done[act[a]] = 1;
+        } else if (iters[act[a]] >= o.niter) {
+          stop[a] = 1;
+        }
+      }
+    }
+    // d += sum_i y_i z_i, y from the triangular system, per system with its own size
+    int mmax = 0;
+    for (int a = 0; a < na; a++) mmax = std::max(mmax, steps[a]);
+    std::vector<double2> y((size_t)mmax * na, make_double2(0, 0));
+    for (int a = 0; a < na; a++) {
+      const int mm = steps[a];
+      std::vector<zc> yv(mm);
+      for (int i = mm - 1; i >= 0; i--) {
+        zc acc = gg[a][i];
+        for (int k2 = i + 1; k2 < mm; k2++) acc -= H[a][(size_t)k2 * (m + 1) + i] * yv[k2];
+        yv[i] = acc / H[a][(size_t)i * (m + 1) + i];
+      }
+      for (int i = 0; i < mm; i++) y[(size_t)i * na + a] = D2(yv[i]);
+    }
+    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, sl.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st));
+    if (mmax > 0)
+      CSEM_CUDA_TRY(cudaMemcpyAsync(cf, y.data(), sizeof(double2) * y.size(), cudaMemcpyHostToDevice, st));
+    for (int i = 0; i < mmax; i++) launch_axpy<F32>(n, na, dl, cf + (size_t)i * na, 1, 0, GZ(i), GD, st);
+    CSEM_CUDA_TRY(cudaGetLastError());
+  }
+}
+
+void MixedBatch::solve_gmres(const std::vector<double>& bn, const double* tol, const MixedOptions& o,
+                             std::vector<MixedResult>& res, std::vector<double>& rnorm, std::vector<int> running)
+{
+  const int m = std::max(1, o.nrestart);
+  const size_t need = sizeof(float2) * (size_t)(2 * m + 4) * nsys * n;
+  if (gm.bytes < need) gm.alloc(need);
+  const size_t needc = sizeof(double2) * (size_t)(m + 2) * nsys;
+  if (gcoef.bytes < needc) gcoef.alloc(needc);
+  const float2* GD = gm.as<float2>() + (size_t)(2 * m + 2) * nsys * n;
+  while (!running.empty()) {
+    std::vector<double> ti;
+    for (int s : running) {
+      const double rel = res[s].outer == 0 ? 1.0 : rnorm[s] / bn[s];
+      ti.push_back(std::min(0.5, std::max(o.inner_tol, 0.5 * tol[s] / rel)));
+    }
+    std::vector<int> it;
+    gmres_inner(running, ti, o, it);
+    for (size_t q = 0; q < running.size(); q++) res[running[q]].inner_iters += it[q];
+    outer_update(running, rnorm, false, GD);
+    std::vector<int> next;
+    for (int s : running) {
+      res[s].outer += 1;
+      const double rel = rnorm[s] / bn[s];
+      res[s].relres = rel;
+      if (rel < tol[s]) res[s].status = ST_CONVERGED;
+      else if (!std::isfinite(rel)) res[s].status = ST_NONFINITE;
+      else if (res[s].inner_iters >= o.max_inner_total || res[s].outer >= o.max_outer) res[s].status = ST_MAXITER;
+      else next.push_back(s);
+    }
+    running = next;
+  }
 }
 
 void MixedBatch::extract(int nch, const int* ch, int nrec, const float* rec, double* out_host)

@@ -1,6 +1,8 @@
 // Batched mixed-precision solver: complex64 inner flexible BiCGStab (LU-SGS or A-phi
 // preconditioned) inside a complex128 defect-correction loop, many systems at once.
 #pragma once
+#include <map>
+#include <tuple>
 #include <vector>
 #include "engine_model.h"
 
@@ -14,6 +16,9 @@ struct MixedOptions {
   double inner_tol = 0.1;   // relative reduction asked of one inner solve
   int check_every = 4;      // inner iterations between host status reads
   bool autotune = false;    // time the LU-SGS sweep variants on the batch, keep the fastest
+  int algopt = 1;           // inner solver: 1 flexible BiCGStab, 2 flexible GMRES(nrestart)
+  bool graphs = true;       // replay the BiCGStab iterations between status reads as CUDA graphs
+  int nrestart = 10;        // GMRES basis size
 };
 
 struct MixedResult {
@@ -26,6 +31,9 @@ struct MixedResult {
 class MixedBatch {
  public:
   MixedBatch(Model* m, int nsys, cudaStream_t st);
+  ~MixedBatch();
+  MixedBatch(const MixedBatch&) = delete;
+  MixedBatch& operator=(const MixedBatch&) = delete;
   Model* m;
   int nsys;
   cudaStream_t st;
@@ -34,6 +42,7 @@ class MixedBatch {
   Ops<F64> o64;
   Ops<F32> o32;
   DevBuf x64, b64, r64, w64, vec32, ks, sc64, sc32, dots, partial, list, rn, srcbuf, chbuf, recbuf, outbuf;
+  DevBuf gm, gcoef;  // GMRES basis (V, Z, w, d, r0) and per-system coefficients
   float2* V(int i) { return vec32.as<float2>() + (size_t)i * nsys * n; }
   // b64 := injected sources (src [nsys][3], iom [nsys] on the host)
   void inject(const float* src, const double* iom, int nch, const int* ch);
@@ -46,9 +55,25 @@ class MixedBatch {
   long inner_launch_iters = 0;  // sum over launched iterations of active systems
  private:
   void inner_iteration(int nact, const int* dlist, int preco, int maxiter);
+  // check_every inner iterations: launched directly the first time a (systems, options)
+  // combination occurs, as a captured CUDA graph from the second time on
+  void inner_iterations(int nact, const MixedOptions& o);
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;   // kernels in it (they count as launches at every replay)
+    int seen = 0;       // times the combination occurred
+    bool failed = false;
+  };
+  std::map<std::tuple<int, int, int, int>, Graph> graphs_;
   void start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner);
   int autotune_lusgs(int nact, const int* dlist);  // returns the chosen points per thread
-  void outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first);
+  void outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first, const float2* d = nullptr);
+  void solve_gmres(const std::vector<double>& bn, const double* tol, const MixedOptions& o,
+                   std::vector<MixedResult>& res, std::vector<double>& rnorm, std::vector<int> running);
+  // one complex64 flexible GMRES(m) inner solve of A d = r/|r| for the systems g
+  void gmres_inner(const std::vector<int>& g, const std::vector<double>& tol_inner, const MixedOptions& o,
+                   std::vector<int>& iters);
+  std::vector<double2> batch_dot(const float2* a, const float2* b, int ng, const int* dl);
 };
 
 }  // namespace csem

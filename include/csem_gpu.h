@@ -101,10 +101,10 @@ int csem_solve_fp64_host(csem_ctx *c, int algopt, int preco, int niter, double t
  * reference driver's per-frequency loop (main.c:93-123: injection, timed solve,
  * extraction) for every (frequency, source) pair at once; the reference itself solves
  * only the first source row (acq_init_free.c:56,90).
- *   precision 32: batched mixed precision - complex64 flexible BiCGStab with complex64
- *                 LU-SGS (preco 1) or A-phi (preco 3) inside complex128 defect
- *                 correction; a system stops when |b - A x| / |b| < tol/f (complex128,
- *                 true residual);
+ *   precision 32: batched mixed precision - complex64 flexible BiCGStab (algopt 1) or
+ *                 flexible GMRES(nrestart) (algopt 2) with complex64 LU-SGS (preco 1)
+ *                 or A-phi (preco 3) inside complex128 defect correction; a system
+ *                 stops when |b - A x| / |b| < tol/f (complex128, true residual);
  *   precision 64: the plain complex128 solver of csem_solve_fp64_host, one system after
  *                 the other (algopt/preco/nrestart/mp as the reference).
  * Outputs per system: dcal [nsys][nchrec][nrec] complex128 receivers, iters (inner
@@ -112,14 +112,14 @@ int csem_solve_fp64_host(csem_ctx *c, int algopt, int preco, int niter, double t
  * correction cycles), status (CSEM_ST_*), relres (final relative residual). */
 typedef struct csem_batch_opts {
   int precision;     /* 32 or 64 */
-  int algopt;        /* 1 BiCGStab, 2 GMRES (precision 64 only) */
+  int algopt;        /* 1 BiCGStab, 2 GMRES */
   int preco;         /* 0 none, 1 LU-SGS, 2 inner GMRES (64 only), 3 A-phi */
   int niter;         /* the reference's niter */
   float tol;         /* the reference's tol; system s stops at tol/freq[s] in float (main.c:94) */
   double inner_tol;  /* precision 32: relative reduction of one inner solve (<= 0: 0.1) */
   int check_every;   /* precision 32: inner iterations between status reads (<= 0: 4) */
   int max_outer;     /* precision 32: defect-correction cycles (<= 0: 30) */
-  int nrestart, mp;  /* precision 64: GMRES(nrestart) and GMRES(mp) preconditioner */
+  int nrestart, mp;  /* GMRES(nrestart); precision 64: GMRES(mp) preconditioner */
 } csem_batch_opts;
 int csem_solve_batch_host(csem_ctx *c, int nsys, const float *freq, const float *src3, int nchsrc,
                           const int *chsrc, int nchrec, const int *chrec, int nrec, const float *rec,
@@ -173,7 +173,11 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     sweep variants (points per thread 1, 2, 4) on its first running
  *                     systems and keeps the fastest for that batch; 0 (default): the
  *                     fixed default. complex64 results may then differ in the last bits
- *                     from run to run, so it is off by default.
+ *                     from run to run, so it is off by default;
+ *   "graphs"          1 (default): the batched BiCGStab replays the iterations between
+ *                     two status reads as a captured CUDA graph (from the second time a
+ *                     given number of systems is running; not while csem_profile is on);
+ *                     0: direct launches.
  */
 int csem_ctx_set_option(csem_ctx *c, const char *name, int value);
 

@@ -111,6 +111,53 @@ def test_mixed_batch_aphi(gpu, small_case):
         assert r["relres"][s] < 1 and r["relres"][s] <= 10 * r64["relres"][s], (r["relres"], r64["relres"])
 
 
+def test_mixed_gmres_matches_fp64(gpu, small_case):
+    """Batched complex64 flexible GMRES(10) inner solves with LU-SGS inside complex128
+    defect correction reach the same answer as the complex128 solver."""
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    rec = cfg.acq.rec
+    r64 = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=64, preco=1, niter=400, tol=1e-8)
+    r32 = cs.solve_batch(ctx, freqs, srcs, rec=rec, precision=32, algopt=2, nrestart=10, preco=1, niter=1000,
+                         tol=1e-8)
+    assert all(s == "converged" for s in r32["status"]), r32
+    for s in range(len(freqs)):
+        assert r32["relres"][s] < float(np.float32(np.float32(1e-8) / freqs[s]))
+        for c in range(3):
+            assert relerr(r32["dcal"][s, c], r64["dcal"][s, c]) <= 1e-6
+
+
+def test_mixed_gmres_aphi(gpu, small_case):
+    """GMRES(10) with A-phi (the combination of the uneven-size batch configuration):
+    the reference's A-phi does not converge on these models, so the batched complex64
+    path is held to the complex128 GMRES's residual after the same budget."""
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    rec = cfg.acq.rec
+    r = cs.solve_batch(ctx, freqs[:2], srcs[:2], rec=rec, precision=32, algopt=2, nrestart=10, preco=3, niter=200,
+                       tol=1e-8, max_outer=1, inner_tol=1e-12)
+    r64 = cs.solve_batch(ctx, freqs[:2], srcs[:2], rec=rec, precision=64, algopt=2, nrestart=10, preco=3, niter=200,
+                         tol=1e-8)
+    for s in range(2):
+        assert r["status"][s] in ("converged", "maxiter"), r["status"]
+        assert np.all(np.isfinite(r["dcal"][s]))
+        assert r["relres"][s] < 1 and r["relres"][s] <= 10 * r64["relres"][s], (r["relres"], r64["relres"])
+
+
+def test_graph_replay_is_bit_identical(gpu, small_case):
+    """The iterations between status reads replayed as CUDA graphs launch the same kernels
+    in the same order as direct launches: identical bits and iteration counts."""
+    cfg, G, ctx, p, src = small_case
+    freqs, srcs = _systems(cfg, src)
+    out = {}
+    for graphs in (1, 0):
+        ctx.set_option("graphs", graphs)
+        out[graphs] = cs.solve_batch(ctx, freqs, srcs, rec=cfg.acq.rec, precision=32, preco=1, niter=400, tol=1e-8)
+    ctx.set_option("graphs", 1)
+    assert np.array_equal(out[1]["dcal"], out[0]["dcal"])
+    assert np.array_equal(out[1]["iters"], out[0]["iters"]) and out[1]["status"] == out[0]["status"]
+
+
 def test_batch_is_deterministic(gpu, small_case):
     cfg, G, ctx, p, src = small_case
     freqs, srcs = _systems(cfg, src)

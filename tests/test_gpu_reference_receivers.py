@@ -1,8 +1,9 @@
-"""Whole solves of the layered 120^3 workload against the reference's own receivers.
+"""Whole solves of the 120^3 workloads against the reference's own receivers.
 
-The fixture tests/golden/layered_120/reference_receivers.npz was computed by the
-reference itself (built from its sources, FFTW replaced by the oracle's DFT) with
-BiCGStab + LU-SGS to tol = 1e-8/f at 0.25, 0.75 and 1.25 Hz. Errors are max-norm
+The fixtures tests/golden/<workload>/reference_receivers.npz (layered_120, and
+vti_block_120 when present) were computed by the reference itself (built from its
+sources, FFTW replaced by the oracle's DFT; tests/golden/make_reference_receivers.py)
+with BiCGStab + LU-SGS to tol = 1e-8/f at 0.25, 0.75 and 1.25 Hz. Errors are max-norm
 relative per frequency and channel. Ey is zero by symmetry on the receiver line (its
 values are rounding noise, about 1e-8 of Ex), so Ey is measured against the Ex max.
 
@@ -25,17 +26,19 @@ from demo_matrixfree_csem_gb300 import synthetic
 
 pytestmark = pytest.mark.gpu
 
-FIX = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "layered_120", "reference_receivers.npz")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+WORKLOADS = [w for w in ("layered_120", "vti_block_120")
+             if os.path.exists(os.path.join(GOLDEN, w, "reference_receivers.npz"))]
 
 
-@pytest.fixture(scope="module")
-def layered(tmp_path_factory):
-    d = str(tmp_path_factory.mktemp("layered"))
-    cfg = synthetic.layered_120()
+@pytest.fixture(scope="module", params=WORKLOADS)
+def layered(request, tmp_path_factory):
+    d = str(tmp_path_factory.mktemp(request.param))
+    cfg = synthetic.workload(request.param)
     synthetic.write_config(cfg, d)
     p = {k: str(v) for k, v in cfg.params.items()}
     G = product_grid(d, p)
-    return cfg, cs.Ctx(G, 1, 0), np.load(FIX)
+    return cfg, cs.Ctx(G, 1, 0), np.load(os.path.join(GOLDEN, request.param, "reference_receivers.npz"))
 
 
 def _errors(dcal, ref):
