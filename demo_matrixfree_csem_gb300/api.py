@@ -88,6 +88,7 @@ def lib(build_if_missing: bool = True):
         "csem_ctx_stream": (C.c_void_p, [C.c_void_p]),
         "csem_ctx_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
         "csem_batch_bytes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp]),
+        "csem_solve_batches_host": (C.c_int, [C.c_int, C.c_void_p]),
         "csem_batch_capacity": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _ip]),
         "csem_fdfd_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_lusgs_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -361,6 +362,48 @@ def solve_batch(ctx: Ctx, freqs, srcs, chsrc=("Ex",), chrec=("Ex", "Ey", "Ez"), 
                                        _p(cr, _ip), len(r), _p(r, _fp), C.byref(o), _p(dcal.view(np.float64)),
                                        _p(it, _ip), _p(ou, _ip), _p(st, _ip), _p(rr)))
     return dict(dcal=dcal, iters=it, outer=ou, status=[STATUS.get(int(v), int(v)) for v in st], relres=rr)
+
+
+class _BatchJob(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("nsys", C.c_int), ("freq", _fp), ("src3", _fp), ("nchsrc", C.c_int),
+                ("chsrc", _ip), ("nchrec", C.c_int), ("chrec", _ip), ("nrec", C.c_int), ("rec", _fp),
+                ("opt", C.POINTER(_BatchOpts)), ("dcal", _dp), ("iters", _ip), ("outer", _ip), ("status", _ip),
+                ("relres", _dp), ("rc", C.c_int)]
+
+
+def solve_batches(jobs):
+    """Solve several batches on distinct contexts at the same time (csem_solve_batches_host).
+    jobs: list of dicts with the arguments of solve_batch (ctx, freqs, srcs and optional
+    keywords). Returns one result dict per job, as solve_batch."""
+    keep, cjobs, outs = [], [], []
+    for j in jobs:
+        j = dict(j)
+        ctx = j.pop("ctx")
+        f = np.ascontiguousarray(j.pop("freqs"), np.float32)
+        sr = np.ascontiguousarray(np.asarray(j.pop("srcs"), np.float32)[:, :3])
+        chsrc = j.pop("chsrc", ("Ex",))
+        chrec = j.pop("chrec", ("Ex", "Ey", "Ez"))
+        rec = j.pop("rec", None)
+        d = dict(precision=32, algopt=1, preco=1, niter=1000, tol=1e-8, inner_tol=0.1, check_every=4, max_outer=30,
+                 nrestart=10, mp=30)
+        d.update(j)
+        o = _BatchOpts(d["precision"], d["algopt"], d["preco"], d["niter"], d["tol"], d["inner_tol"],
+                       d["check_every"], d["max_outer"], d["nrestart"], d["mp"])
+        cs_ = np.asarray([CHANNELS[c] if isinstance(c, str) else c for c in chsrc], np.int32)
+        cr = np.asarray([CHANNELS[c] if isinstance(c, str) else c for c in chrec], np.int32)
+        r = np.ascontiguousarray(rec if rec is not None else np.zeros((0, 5)), np.float32)
+        nsys = len(f)
+        out = dict(dcal=np.zeros((nsys, len(cr), len(r)), np.complex128), iters=np.zeros(nsys, np.int32),
+                   outer=np.zeros(nsys, np.int32), st=np.zeros(nsys, np.int32), relres=np.zeros(nsys))
+        keep += [f, sr, cs_, cr, r, o]
+        outs.append(out)
+        cjobs.append(_BatchJob(ctx.h, nsys, _p(f, _fp), _p(sr, _fp), len(cs_), _p(cs_, _ip), len(cr), _p(cr, _ip),
+                               len(r), _p(r, _fp), C.pointer(o), _p(out["dcal"].view(np.float64)),
+                               _p(out["iters"], _ip), _p(out["outer"], _ip), _p(out["st"], _ip), _p(out["relres"]), 0))
+    arr = (_BatchJob * len(cjobs))(*cjobs)
+    _check(lib().csem_solve_batches_host(len(cjobs), arr))
+    return [dict(dcal=o["dcal"], iters=o["iters"], outer=o["outer"],
+                 status=[STATUS.get(int(v), int(v)) for v in o["st"]], relres=o["relres"]) for o in outs]
 
 
 PROF_NAMES = ["A64", "A32", "lusgs64", "lusgs32", "aphi64", "aphi32", "air64", "air32", "stencil64", "stencil32"]

@@ -2,6 +2,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <string>
+#include <system_error>
+#include <thread>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -216,6 +219,39 @@ int csem_batch_capacity(csem_ctx* c, int precision, int preco, double budget_byt
   }
   const double one = batch_bytes(c->model, 32, preco, 1);
   *nsys = one > 0 ? (int)std::min(1.0e9, std::floor(budget_bytes / one)) : 0;
+  return CSEM_OK;
+}
+
+int csem_solve_batches_host(int njobs, csem_batch_job* jobs)
+{
+  if (njobs < 0 || (njobs > 0 && !jobs)) return csem_set_error(CSEM_EINVAL, "csem_solve_batches_host: bad arguments");
+  for (int a = 0; a < njobs; a++) {
+    if (!jobs[a].ctx) return csem_set_error(CSEM_EINVAL, "csem_solve_batches_host: job %d has no context", a);
+    for (int b = 0; b < a; b++)
+      if (jobs[a].ctx == jobs[b].ctx)
+        return csem_set_error(CSEM_EINVAL, "csem_solve_batches_host: jobs %d and %d share a context", b, a);
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return csem_set_error(CSEM_ENODEV, "no CUDA device available");
+  std::vector<std::string> msgs(njobs);
+  auto run = [&](int a) {
+    cudaSetDevice(dev);
+    csem_batch_job& j = jobs[a];
+    j.rc = csem_solve_batch_host(j.ctx, j.nsys, j.freq, j.src3, j.nchsrc, j.chsrc, j.nchrec, j.chrec, j.nrec, j.rec,
+                                 j.opt, j.dcal, j.iters, j.outer, j.status, j.relres);
+    if (j.rc) msgs[a] = csem_last_error();  // the message lives in this thread
+  };
+  std::vector<std::thread> th;
+  try {
+    for (int a = 1; a < njobs; a++) th.emplace_back(run, a);
+  } catch (const std::system_error&) {
+    for (auto& t : th) t.join();
+    return csem_set_error(CSEM_ENOMEM, "csem_solve_batches_host: cannot start threads");
+  }
+  if (njobs > 0) run(0);
+  for (auto& t : th) t.join();
+  for (int a = 0; a < njobs; a++)
+    if (jobs[a].rc) return csem_set_error(jobs[a].rc, "job %d: %s", a, msgs[a].c_str());
   return CSEM_OK;
 }
 
@@ -608,7 +644,7 @@ int csem_cdot_dev(int prec, long n, int nsys, const void* a, const void* b, doub
   if (prec != 64 && prec != 32) return csem_set_error(CSEM_EINVAL, "prec must be 64 or 32");
   API_BEGIN
   const int nblk = dot_blocks(n);
-  static DevBuf part;
+  static thread_local DevBuf part;  // callers on different threads use different streams
   ensure(part, sizeof(double2) * (size_t)nblk * nsys);
   if (prec == 64)
     launch_dot<F64>((const double2*)a, (const double2*)b, n, n, nsys, nullptr, part.as<double2>(), nblk,

@@ -105,6 +105,8 @@ Model::Model(const csem_grid* gp, int airbc_, int fvm_)
   if (airbc) {
     N1 = G.n1fft;
     N2 = G.n2fft;
+    fft_plans.N1 = N1;
+    fft_plans.N2 = N2;
     // gather tables (airbc_init_free.c:90-105), -1 where the reference writes zero
     std::vector<int> ih;  // jx[N1], jy[N2], hx_j1[n1+1], hx_j2[n2], hy_j1[n1], hy_j2[n2+1]
     std::vector<double> wh;
@@ -226,19 +228,6 @@ void FftPlans::exec(bool dbl, void* data, int count, int dir, cudaStream_t st)
   }
 }
 
-FftPlans* fft_plans_for(int N1, int N2)
-{
-  static std::map<std::pair<int, int>, FftPlans*> cache;
-  auto key = std::make_pair(N1, N2);
-  auto it = cache.find(key);
-  if (it != cache.end()) return it->second;
-  FftPlans* p = new FftPlans();
-  p->N1 = N1;
-  p->N2 = N2;
-  cache[key] = p;
-  return p;
-}
-
 SysScal<F64> sys_scal64(double iom_re, double iom_im)
 {
   // 1/(I omega mu0) as the reference computes it (fdfd.c:100): real over complex,
@@ -294,7 +283,7 @@ Ops<P>::Ops(Model* m_, int nslot_max, cudaStream_t st_) : m(m_), nmax(nslot_max)
     ghy.alloc(cs * (size_t)m->n1 * (m->n2 + 1) * nmax);
     const long capE = (long)m->nb * ((long)m->n1 * (m->n2 + 1) + (long)(m->n1 + 1) * m->n2 + (long)(m->n1 + 1) * (m->n2 + 1));
     cap.alloc(cs * (size_t)capE * nmax);
-    fft = fft_plans_for(m->N1, m->N2);
+    fft = &m->fft_plans;
   }
 }
 

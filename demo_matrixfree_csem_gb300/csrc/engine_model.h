@@ -65,6 +65,9 @@ class Model {
   AirP<F64> a64;
   AirP<F32> a32;
   AcqGrid acq;
+  // cuFFT plans of this model's airwave grid (one set per model: a plan is bound to one
+  // stream at a time, and contexts may run on different host threads)
+  FftPlans fft_plans;
   template <class P> const GridP<P>& grid() const;
   template <class P> const AirP<P>& air() const;
   template <class P> GridP<P> grid_shifted() const;  // d3/sigma advanced by kstart planes
@@ -93,7 +96,6 @@ class Ops {
   ~Ops();
 };
 
-FftPlans* fft_plans_for(int N1, int N2);
 
 SysScal<F64> sys_scal64(double iom_re, double iom_im);
 SysScal<F32> sys_scal32(const SysScal<F64>& s);

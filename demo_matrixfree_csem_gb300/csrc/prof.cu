@@ -1,4 +1,6 @@
 // Per-operator device timing (see prof.h) and its C entry points.
+#include <atomic>
+#include <mutex>
 #include <vector>
 #include "../../include/csem_gpu.h"
 #include "prof.h"
@@ -11,7 +13,8 @@ struct Rec {
   cudaEvent_t a, b;
   bool closed;
 };
-bool g_on = false;
+std::atomic<bool> g_on{false};
+std::mutex g_mu;  // records may come from several host threads (one per context)
 std::vector<Rec> g_recs;
 std::vector<cudaEvent_t> g_pool;
 
@@ -28,13 +31,14 @@ cudaEvent_t get_event()
 }
 }  // namespace
 
-static long long g_launches = 0;
+static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches += n; }
 
 bool prof_on() { return g_on; }
 
 int prof_begin(int cat, cudaStream_t st, int units)
 {
+  std::lock_guard<std::mutex> lock(g_mu);
   Rec r;
   r.cat = cat;
   r.units = units;
@@ -48,6 +52,7 @@ int prof_begin(int cat, cudaStream_t st, int units)
 
 void prof_end(int tok, cudaStream_t st)
 {
+  std::lock_guard<std::mutex> lock(g_mu);
   if (tok < 0 || tok >= (int)g_recs.size()) return;
   cudaEventRecord(g_recs[tok].b, st);
   g_recs[tok].closed = true;
@@ -62,6 +67,7 @@ int csem_profile(int enable)
 {
   using namespace csem;
   cudaDeviceSynchronize();
+  std::lock_guard<std::mutex> lock(g_mu);
   for (auto& r : g_recs) {
     g_pool.push_back(r.a);
     g_pool.push_back(r.b);
@@ -80,6 +86,7 @@ int csem_profile_read(int ncat, double* ms, long* count, long* units)
 {
   using namespace csem;
   cudaDeviceSynchronize();
+  std::lock_guard<std::mutex> lock(g_mu);
   for (int c = 0; c < ncat; c++) {
     ms[c] = 0;
     count[c] = 0;

@@ -230,6 +230,79 @@ def large_420(seed: int = 2, freqs=(0.125, 0.25, 0.5, 0.75, 1.0, 1.25), nsrc: in
     return Config(model, Acquisition(src, rec), params, name="large_420")
 
 
+def _layered_cells(x3, surfaces, rho_layers):
+    """Cell resistivities of layers separated by depth surfaces ([ny][nx] each, top to
+    bottom), averaged over each cell's vertical extent: conductivity arithmetically for
+    the horizontal components and resistivity arithmetically for the vertical one (the
+    volume-fraction averaging of the reference's bathymetry example,
+    bathymetry/main.c:25-104). Returns rho_h, rho_v as float32 [nz][ny][nx]."""
+    ztop = np.asarray(x3[:-1], np.float64)[:, None, None]
+    zbot = np.asarray(x3[1:], np.float64)[:, None, None]
+    dz = zbot - ztop
+    cuts = [None] + [np.asarray(sf, np.float64)[None] for sf in surfaces] + [None]
+    sig = np.zeros((len(ztop),) + np.shape(surfaces[0]))
+    rv = np.zeros_like(sig)
+    for L, rho in enumerate(rho_layers):
+        lo = ztop if cuts[L] is None else np.maximum(ztop, cuts[L])
+        hi = zbot if cuts[L + 1] is None else np.minimum(zbot, cuts[L + 1])
+        frac = np.clip(hi - lo, 0.0, None) / dz
+        sig += frac / rho
+        rv += frac * rho
+    return (1.0 / sig).astype(np.float32), rv.astype(np.float32)
+
+
+def bathymetry_125(seed: int = 1, freqs=(0.25, 0.75, 1.25), nsrc: int = 8) -> Config:
+    """125x125x100 cells of 100 m; seafloor at 1000 m plus 3 seeded Gaussian hills
+    (amplitude 200-500 m, sigma 1-3 km); 0.3 ohm-m water above it, 1 ohm-m below, and a
+    30 ohm-m layer 100 m thick following the topography 800 m beneath it; partial cells
+    averaged by volume fraction. Ex sources every 1 km on y=0, 50 m above the local
+    seafloor; receivers on the seafloor along y=0 every 200 m."""
+    rng = np.random.default_rng(seed)
+    x1 = np.arange(-6250, 6251, 100, dtype=np.float32)
+    x2 = x1.copy()
+    x3 = np.arange(0, 10001, 100, dtype=np.float32)
+    xc, yc = _centres(x1), _centres(x2)
+    X, Y = np.meshgrid(xc, yc)
+    hills = [(rng.uniform(200, 500), rng.uniform(1000, 3000), rng.uniform(-4000, 4000), rng.uniform(-4000, 4000))
+             for _ in range(3)]
+
+    def seafloor(x, y):
+        return 1000.0 + sum(a * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * sg * sg)) for a, sg, cx, cy in hills)
+
+    sf = seafloor(X, Y)
+    rh, rv = _layered_cells(x3, [sf, sf + 800.0, sf + 900.0], [0.3, 1.0, 30.0, 1.0])
+    model = Model(x1, x2, x3, rh, rh.copy(), rv, name="bathymetry_125")
+    sx = -3500.0 + 1000.0 * np.arange(nsrc)
+    src = np.stack([sx, np.zeros(nsrc), seafloor(sx, 0.0) - 50.0, np.zeros(nsrc), np.zeros(nsrc)],
+                   axis=1).astype(np.float32)
+    rx = np.arange(-6000, 6001, 200, dtype=np.float64)
+    rec = np.stack([rx, np.zeros_like(rx), seafloor(rx, 0.0), np.zeros_like(rx), np.zeros_like(rx)],
+                   axis=1).astype(np.float32)
+    params = dict(airbc=1, nb=10, lextend="40e3", preco=3, algopt=2, nrestart=10, tol="1e-8", niter=1000,
+                  fvm=0, chsrc="Ex", chrec="Ex,Ey,Ez", freqs=",".join(str(f) for f in freqs))
+    return Config(model, Acquisition(src, rec), params, name="bathymetry_125")
+
+
+def layered_64(freqs=(0.25, 0.75, 1.25)) -> Config:
+    """64^3 cells of 100 m: 0.3 ohm-m water above 1000 m, 1 ohm-m below, 100 ohm-m at
+    2000-2100 m; one Ex dipole at (0, 0, 950) and seafloor receivers along y=0."""
+    x1 = np.arange(-3200, 3201, 100, dtype=np.float32)
+    x2 = x1.copy()
+    x3 = np.arange(0, 6401, 100, dtype=np.float32)
+    zc = _centres(x3)
+    rz = np.where(zc < 1000, 0.3, 1.0)
+    rz = np.where((zc >= 2000) & (zc < 2100), 100.0, rz)
+    rho = np.broadcast_to(rz[:, None, None], (64, 64, 64)).astype(np.float32)
+    model = Model(x1, x2, x3, rho.copy(), rho.copy(), rho.copy(), name="layered_64")
+    src = np.array([[0, 0, 950, 0, 0]], dtype=np.float32)
+    rx = np.arange(-3000, 3001, 100, dtype=np.float64)
+    rec = np.stack([rx, np.zeros_like(rx), np.full_like(rx, 1000.0), np.zeros_like(rx), np.zeros_like(rx)],
+                   axis=1).astype(np.float32)
+    params = dict(airbc=1, nb=10, lextend="40e3", preco=3, algopt=2, nrestart=10, tol="1e-8", niter=1000,
+                  fvm=0, chsrc="Ex", chrec="Ex,Ey,Ez", freqs=",".join(str(f) for f in freqs))
+    return Config(model, Acquisition(src, rec), params, name="layered_64")
+
+
 def random_small(seed: int, nx=12, ny=10, nz=9, airbc=0, nb=3, aniso=True, stretch=True,
                  freqs=(0.5, 1.0), **extra) -> Config:
     """Small random model: random (optionally stretched) node spacings, random
@@ -274,11 +347,13 @@ def random_small(seed: int, nx=12, ny=10, nz=9, airbc=0, nb=3, aniso=True, stret
 
 
 WORKLOADS = {"marlim_like_96": lambda: marlim_like(seed=0), "layered_120": layered_120,
-             "vti_block_120": vti_block_120, "large_420_192": lambda: large_420(seed=2)}
+             "vti_block_120": vti_block_120, "large_420_192": lambda: large_420(seed=2),
+             "bathymetry_125": bathymetry_125, "layered_64": layered_64}
 
 
 def workload(name: str) -> Config:
-    """A named benchmark workload (marlim_like_96, layered_120, vti_block_120, large_420_192)."""
+    """A named workload (marlim_like_96, layered_120, vti_block_120, large_420_192,
+    bathymetry_125, layered_64)."""
     if name not in WORKLOADS:
         raise ValueError(f"unknown workload {name}; known: {', '.join(WORKLOADS)}")
     return WORKLOADS[name]()

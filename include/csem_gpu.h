@@ -126,6 +126,32 @@ int csem_solve_batch_host(csem_ctx *c, int nsys, const float *freq, const float 
                           const csem_batch_opts *opt, double *dcal, int *iters, int *outer, int *status,
                           double *relres);
 
+/* ------------------------------------------------------------ several models at once
+ * Solve independent batches on different contexts (different models, grid sizes or
+ * padding) at the same time: one host thread per job drives that context's
+ * csem_solve_batch_host on the context's own stream, so the GPU overlaps the contexts'
+ * kernels. This is the uneven-size batch of several models (e.g. one context per model
+ * and per padding); the reference solves one system of one model at a time (main.c:93-123).
+ * Each job names a distinct context; rc receives that job's return code. Returns CSEM_OK
+ * when every job succeeded, else the first failing job's code. */
+typedef struct csem_batch_job {
+  csem_ctx *ctx;
+  int nsys;
+  const float *freq, *src3;
+  int nchsrc;
+  const int *chsrc;
+  int nchrec;
+  const int *chrec;
+  int nrec;
+  const float *rec;
+  const csem_batch_opts *opt;
+  double *dcal;
+  int *iters, *outer, *status;
+  double *relres;
+  int rc;
+} csem_batch_job;
+int csem_solve_batches_host(int njobs, csem_batch_job *jobs);
+
 /* Capacity planning for large sets of systems (no counterpart in the reference, which
  * solves one system at a time). csem_batch_bytes: device bytes csem_solve_batch_host
  * needs for nsys systems with this precision and preconditioner, beyond the model and

@@ -158,6 +158,32 @@ def test_graph_replay_is_bit_identical(gpu, small_case):
     assert np.array_equal(out[1]["iters"], out[0]["iters"]) and out[1]["status"] == out[0]["status"]
 
 
+def test_concurrent_contexts_match_separate_solves(gpu, tmp_path):
+    """Uneven-size batch: three models of different grid sizes (and paddings) on three
+    contexts, solved at the same time by csem_solve_batches_host (one host thread and one
+    stream per context), give exactly the results of solving each context alone."""
+    ctxs, cfgs = [], []
+    for q, (nx, ny, nz, nb) in enumerate([(24, 20, 14, 4), (30, 18, 12, 3), (20, 26, 16, 5)]):
+        cfg = synthetic.random_small(70 + q, nx=nx, ny=ny, nz=nz, nb=nb, airbc=1, n1fft=64, n2fft=64)
+        d = tmp_path / f"m{q}"
+        d.mkdir()
+        synthetic.write_config(cfg, str(d))
+        p = {k: str(v) for k, v in cfg.params.items()}
+        ctxs.append(cs.Ctx(product_grid(str(d), p), 1, 0))
+        cfgs.append(cfg)
+    jobs = []
+    for q, (ctx, cfg) in enumerate(zip(ctxs, cfgs)):
+        srcs = np.stack([cfg.acq.src[0], cfg.acq.src[0] + np.array([19.0, 11.0, 0, 0, 0], np.float32)])
+        jobs.append(dict(ctx=ctx, freqs=np.array([0.5, 1.0], np.float32), srcs=srcs, rec=cfg.acq.rec, niter=400,
+                         tol=1e-8, algopt=1 + (q % 2), nrestart=10))
+    together = cs.solve_batches(jobs)
+    for j, got in zip(jobs, together):
+        args = {k: v for k, v in j.items() if k not in ("ctx", "freqs", "srcs")}
+        alone = cs.solve_batch(j["ctx"], j["freqs"], j["srcs"], **args)
+        assert got["status"] == alone["status"] == ["converged", "converged"]
+        assert np.array_equal(got["dcal"], alone["dcal"]) and np.array_equal(got["iters"], alone["iters"])
+
+
 def test_batch_is_deterministic(gpu, small_case):
     cfg, G, ctx, p, src = small_case
     freqs, srcs = _systems(cfg, src)
