@@ -31,6 +31,7 @@ struct csem_ctx {
   int lusgs_vw = 0;
   bool autotune = false;
   bool graphs = true;
+  bool seq_dots = false;
 };
 
 // the context's kernel-schedule options on one operator set
@@ -163,12 +164,20 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     c->autotune = value != 0;
   } else if (!strcmp(name, "graphs")) {
     c->graphs = value != 0;
+  } else if (!strcmp(name, "dot_order")) {
+    if (value != 0 && value != 1) return csem_set_error(CSEM_EINVAL, "dot_order must be 0 (tree) or 1 (reference)");
+    c->seq_dots = value == 1;
+  } else if (!strcmp(name, "fix_quirks")) {
+    c->model->acq.fix_src_sigma = value != 0;
   } else {
     return csem_set_error(CSEM_EINVAL, "unknown option %s", name);
   }
   if (c->ops64) configure(c, *c->ops64);
   if (c->ops32) configure(c, *c->ops32);
-  if (c->solver) configure(c, c->solver->ops);
+  if (c->solver) {
+    configure(c, c->solver->ops);
+    c->solver->seq_dots = c->seq_dots;
+  }
   if (c->batch) {
     configure(c, c->batch->o64);
     configure(c, c->batch->o32);
@@ -194,8 +203,8 @@ static double batch_bytes(const Model* m, int precision, int preco, int nsys)
     return b;
   };
   if (precision == 32) {
-    // x, b, r, w in complex128; 8 complex64 Krylov vectors; per-system scalars
-    return nsys * (4.0 * 16 * lE + 8.0 * 8 * lE + ops(16) + ops(8) + 4096.0);
+    // x, b, r, w in complex128; 9 complex64 Krylov vectors; per-system scalars
+    return nsys * (4.0 * 16 * lE + 9.0 * 8 * lE + ops(16) + ops(8) + 4096.0);
   }
   // the complex128 solver runs one system at a time: 7 BiCGStab vectors or GMRES(m) bases
   return 16.0 * lE * 40 + ops(16);
@@ -350,6 +359,7 @@ static Solver64* solver_for(csem_ctx* c)
   if (!c->solver) {
     c->solver = new Solver64(c->model, c->st);
     configure(c, c->solver->ops);
+    c->solver->seq_dots = c->seq_dots;
   }
   return c->solver;
 }

@@ -79,6 +79,15 @@ void launch_aphi_grad(const SweepP<P>& s, const typename P::C* V, int nslot, cud
 template <class P>
 void launch_dot(const typename P::C* a, const typename P::C* b, long n, long stride, int nslot,
                 const int* sys_list, double2* partial, int nblk, double2* out, cudaStream_t st);
+// out1 = a1.conj(b1), out2 = a2.conj(b2) in one pass, each bit-identical to launch_dot;
+// partial holds 2 * nslot * nblk entries
+template <class P>
+void launch_dot2(const typename P::C* a1, const typename P::C* b1, const typename P::C* a2,
+                 const typename P::C* b2, long n, long stride, int nslot, const int* sys_list, double2* partial,
+                 int nblk, double2* out1, double2* out2, cudaStream_t st);
+// complex128 <a, b> of one system in the reference's sequential order (bit-identical to
+// cdotprod.c), into out[0]; one CTA, a dependent chain of n additions
+void launch_dot_seq(const double2* a, const double2* b, long n, double2* out, cudaStream_t st);
 int dot_blocks(long n);
 
 }  // namespace csem

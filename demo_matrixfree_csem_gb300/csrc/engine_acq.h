@@ -10,6 +10,7 @@ struct AcqGrid {
   const double *x1, *x2, *x3, *x1s, *x2s, *x3s;
   const double *s11, *s22, *s33;    // full-grid conductivities
   float rho_water;
+  int fix_src_sigma;  // 1: the source's conductivity at its own row (not the reference's -nb shift)
 };
 
 void launch_inject(const AcqGrid& g, int nslot, const float* src, const double2* iom, const int* ch, int nch,

@@ -99,6 +99,7 @@ Model::Model(const csem_grid* gp, int airbc_, int fvm_)
   acq.x1 = xd; acq.x2 = xd + L; acq.x3 = xd + 2 * L; acq.x1s = xd + 3 * L; acq.x2s = xd + 4 * L; acq.x3s = xd + 5 * L;
   acq.s11 = g64.s11; acq.s22 = g64.s22; acq.s33 = g64.s33;
   acq.rho_water = rho_water;
+  acq.fix_src_sigma = 0;
 
   memset(&a64, 0, sizeof(a64));
   memset(&a32, 0, sizeof(a32));
@@ -283,6 +284,7 @@ Ops<P>::Ops(Model* m_, int nslot_max, cudaStream_t st_) : m(m_), nmax(nslot_max)
     ghy.alloc(cs * (size_t)m->n1 * (m->n2 + 1) * nmax);
     const long capE = (long)m->nb * ((long)m->n1 * (m->n2 + 1) + (long)(m->n1 + 1) * m->n2 + (long)(m->n1 + 1) * (m->n2 + 1));
     cap.alloc(cs * (size_t)capE * nmax);
+    CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, cap.bytes, st));  // its boundary planes stay zero
     fft = &m->fft_plans;
   }
 }
@@ -321,7 +323,7 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
 }
 
 template <class P>
-void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
+void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, bool bounds_zero)
 {
   ProfScope prof(P::exact ? PROF_LUSGS64 : PROF_LUSGS32, st, nslot);
   SweepP<P> s;
@@ -339,9 +341,9 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
     s.capEx = (long)nb * n1 * (n2 + 1);
     s.capEy = (long)nb * (n1 + 1) * n2;
     s.capE = s.capEx + s.capEy + (long)nb * (n1 + 1) * (n2 + 1);
-    CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, sizeof(C) * (size_t)s.capE * nslot, st));
+    if (!bounds_zero) CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, sizeof(C) * (size_t)s.capE * nslot, st));
   }
-  zero(Y, m->lE, nslot, sys_list);
+  if (!bounds_zero) zero(Y, m->lE, nslot, sys_list);
   // both schedules visit the points of a sweep in an order that respects every
   // dependency of the lexicographic sweep, so they may be mixed sweep by sweep
   auto sweep = [&](int comp, bool fwd) {

@@ -90,7 +90,12 @@ class Ops {
   int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
   // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal)
   void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
-  void apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
+  // bounds_zero: the caller guarantees that Y's entries outside the swept interior are
+  // zero (they are never written by the sweeps, so a buffer only ever written by
+  // apply_lusgs, or by operations that keep them zero, stays so); then Y is not cleared
+  // first. The sweeps overwrite every interior point before reading it.
+  void apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
+                   bool bounds_zero = false);
   void apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
   void zero(C* Y, long n, int nslot, const int* sys_list);
   ~Ops();

@@ -7,7 +7,8 @@
 // Reference behaviours kept on purpose: with airbc the source's conductivity lookup is
 // made after shifting k by -nb (so it reads nb rows higher in the air-included array,
 // inject_extract.c:55-63), while the Ez receiver uses the unshifted row
-// (inject_extract.c:194-206).
+// (inject_extract.c:194-206). AcqGrid::fix_src_sigma = 1 (the context option "fix_quirks")
+// looks the source's conductivity up at its own row of the air-included array instead.
 #include "csem_cuda.cuh"
 #include "engine_acq.h"
 
@@ -70,14 +71,15 @@ __global__ void k_inject(AcqGrid g, int nslot, const float* __restrict__ src, co
     if (c < 2) sv = cdivr<F64>(sv, (double)g.rho_water);
     int k = q.k - (g.airbc ? g.nb : 0);
     if (k < 0) continue;  // above the operator grid (the host rejects such positions first)
+    const int ksig = g.fix_src_sigma ? q.k : k;  // row of the conductivity lookup
     for (int m = 0; m < 8; m++) {
       const int di = m & 1, dj = (m >> 1) & 1, dk = m >> 2;
       const double a1 = di ? q.w1 : __dsub_rn(1., q.w1), a2 = dj ? q.w2 : __dsub_rn(1., q.w2),
                    a3 = dk ? q.w3 : __dsub_rn(1., q.w3);
       const int kk = k + dk, jj = q.j + dj, ii = q.i + di;
       double2 v;
-      if (c == 0) v = cdivr<F64>(sv, g.s11[ix1(g.n1, g.n2, kk, jj, ii)]);
-      else if (c == 1) v = cdivr<F64>(sv, g.s22[ix2(g.n1, g.n2, kk, jj, ii)]);
+      if (c == 0) v = cdivr<F64>(sv, g.s11[ix1(g.n1, g.n2, ksig + dk, jj, ii)]);
+      else if (c == 1) v = cdivr<F64>(sv, g.s22[ix2(g.n1, g.n2, ksig + dk, jj, ii)]);
       else v = sv;
       v = rmul<F64>(a3, rmul<F64>(a2, rmul<F64>(a1, v)));
       const long p = eidx(g, c, kk, jj, ii);

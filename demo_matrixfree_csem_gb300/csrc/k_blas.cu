@@ -74,6 +74,31 @@ __device__ __forceinline__ double2 block_sum(double2 v)
   return v;
 }
 
+// One thread's share of sum a*conj(b) over [beg, end) with stride DOT_THREADS.
+template <class P> struct DotAcc;
+template <> struct DotAcc<F64> {
+  double2 acc = make_double2(0, 0);
+  __device__ __forceinline__ void add(double2 a, double2 b)
+  {
+    double2 x = make_double2(a.x, a.y), y = make_double2(b.x, -b.y);
+    double2 pr = cmul<F64>(x, y);
+    acc.x = __dadd_rn(acc.x, pr.x);
+    acc.y = __dadd_rn(acc.y, pr.y);
+  }
+  __device__ __forceinline__ double2 value() const { return acc; }
+};
+template <> struct DotAcc<F32> {
+  Acc2 re = {0.f, 0.f}, im = {0.f, 0.f};
+  __device__ __forceinline__ void add(float2 a, float2 b)
+  {
+    re.addprod(a.x, b.x);
+    re.addprod(a.y, b.y);
+    im.addprod(a.y, b.x);
+    im.subprod(a.x, b.y);
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2(re.value(), im.value()); }
+};
+
 // partial[slot][blk] = sum over the block's chunk of a*conj(b)
 template <class P>
 __global__ void __launch_bounds__(DOT_THREADS)
@@ -86,28 +111,38 @@ k_dot_partial(const typename P::C* __restrict__ A, const typename P::C* __restri
   const typename P::C* b = B + (size_t)sys * stride;
   const long chunk = (n + nblk - 1) / nblk;
   const long beg = (long)blockIdx.x * chunk, end = min(n, beg + chunk);
-  double2 acc;
-  if (P::exact) {
-    acc = make_double2(0, 0);
-    for (long q = beg + threadIdx.x; q < end; q += DOT_THREADS) {
-      double2 x = make_double2((double)a[q].x, (double)a[q].y), y = make_double2((double)b[q].x, -(double)b[q].y);
-      double2 pr = cmul<F64>(x, y);
-      acc.x = __dadd_rn(acc.x, pr.x);
-      acc.y = __dadd_rn(acc.y, pr.y);
-    }
-  } else {
-    Acc2 re = {0.f, 0.f}, im = {0.f, 0.f};
-    for (long q = beg + threadIdx.x; q < end; q += DOT_THREADS) {
-      const float ar = (float)a[q].x, ai = (float)a[q].y, br = (float)b[q].x, bi = (float)b[q].y;
-      re.addprod(ar, br);
-      re.addprod(ai, bi);
-      im.addprod(ai, br);
-      im.subprod(ar, bi);
-    }
-    acc = make_double2(re.value(), im.value());
-  }
-  acc = block_sum(acc);
+  DotAcc<P> d;
+  for (long q = beg + threadIdx.x; q < end; q += DOT_THREADS) d.add(a[q], b[q]);
+  const double2 acc = block_sum(d.value());
   if (threadIdx.x == 0) partial[(size_t)slot * nblk + blockIdx.x] = acc;
+}
+
+// Two dot products a1*conj(b1) and a2*conj(b2) in one pass, with the partition, per-thread
+// order and tree of k_dot_partial, so each equals its single-dot result bit for bit.
+// Vectors the two share (s.t and t.t, r.r and r.r0) are read from DRAM once.
+// partial[slot][blk] and partial[nslot + slot][blk].
+template <class P>
+__global__ void __launch_bounds__(DOT_THREADS)
+k_dot2_partial(const typename P::C* __restrict__ A1, const typename P::C* __restrict__ B1,
+               const typename P::C* __restrict__ A2, const typename P::C* __restrict__ B2, long n, long stride,
+               const int* __restrict__ sys_list, double2* __restrict__ partial, int nblk)
+{
+  const int slot = blockIdx.y;
+  const int sys = sys_list ? sys_list[slot] : slot;
+  const size_t so = (size_t)sys * stride;
+  const long chunk = (n + nblk - 1) / nblk;
+  const long beg = (long)blockIdx.x * chunk, end = min(n, beg + chunk);
+  DotAcc<P> d1, d2;
+  for (long q = beg + threadIdx.x; q < end; q += DOT_THREADS) {
+    d1.add(A1[so + q], B1[so + q]);
+    d2.add(A2[so + q], B2[so + q]);
+  }
+  const double2 acc1 = block_sum(d1.value());
+  const double2 acc2 = block_sum(d2.value());
+  if (threadIdx.x == 0) {
+    partial[(size_t)slot * nblk + blockIdx.x] = acc1;
+    partial[(size_t)(gridDim.y + slot) * nblk + blockIdx.x] = acc2;
+  }
 }
 
 __global__ void k_dot_final(const double2* __restrict__ partial, int nblk, double2* __restrict__ out)
@@ -123,6 +158,68 @@ __global__ void k_dot_final(const double2* __restrict__ partial, int nblk, doubl
   if (threadIdx.x == 0) out[slot] = acc;
 }
 
+// out1[slot], out2[slot] from the two partial sets of k_dot2_partial (k_dot_final's order)
+__global__ void k_dot2_final(const double2* __restrict__ partial, int nblk, double2* __restrict__ out1,
+                             double2* __restrict__ out2)
+{
+  const int slot = blockIdx.x;
+  for (int h = 0; h < 2; h++) {
+    const double2* pp = partial + (size_t)(h * gridDim.x + slot) * nblk;
+    double2 acc = make_double2(0, 0);
+    for (int q = threadIdx.x; q < nblk; q += DOT_THREADS) {
+      double2 v = pp[q];
+      acc.x = __dadd_rn(acc.x, v.x);
+      acc.y = __dadd_rn(acc.y, v.y);
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) (h ? out2 : out1)[slot] = acc;
+  }
+}
+
+// complex128 <a, b> in the reference's order (cdotprod.c:13-19): s += a_i conj(b_i) from
+// i = 0 to n-1, each product and each addition rounded once, so the result is the
+// reference's bit for bit. The sum is one dependent chain per component: thread 0 adds
+// a chunk of products from shared memory while the other threads form the next chunk's
+// products (coalesced loads), one CTA per call.
+static constexpr int SEQ_CHUNK = 2048;
+
+__global__ void __launch_bounds__(DOT_THREADS)
+k_dot_seq(const double2* __restrict__ a, const double2* __restrict__ b, long n, double2* __restrict__ out)
+{
+  __shared__ double2 prod[2][SEQ_CHUNK];
+  const long nch = (n + SEQ_CHUNK - 1) / SEQ_CHUNK;
+  auto fill = [&](long c, int first, int step) {
+    double2* pb = prod[c & 1];
+    for (int t = first; t < SEQ_CHUNK; t += step) {
+      const long q = c * SEQ_CHUNK + t;
+      if (q < n) pb[t] = cmul<F64>(a[q], make_double2(b[q].x, -b[q].y));
+    }
+  };
+  if (nch > 0) fill(0, threadIdx.x, DOT_THREADS);
+  __syncthreads();
+  double sr = 0.0, si = 0.0;
+  for (long c = 0; c < nch; c++) {
+    if (threadIdx.x == 0) {
+      const double2* pb = prod[c & 1];
+      const int m = (int)min((long)SEQ_CHUNK, n - c * SEQ_CHUNK);
+      for (int t = 0; t < m; t++) {
+        const double2 v = pb[t];
+        sr = __dadd_rn(sr, v.x);
+        si = __dadd_rn(si, v.y);
+      }
+    } else if (c + 1 < nch) {
+      fill(c + 1, threadIdx.x - 1, DOT_THREADS - 1);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = make_double2(sr, si);
+}
+
+void launch_dot_seq(const double2* a, const double2* b, long n, double2* out, cudaStream_t st)
+{
+  count_launch(), k_dot_seq<<<1, DOT_THREADS, 0, st>>>(a, b, n, out);
+}
+
 template <class P>
 void launch_dot(const typename P::C* a, const typename P::C* b, long n, long stride, int nslot,
                 const int* sys_list, double2* partial, int nblk, double2* out, cudaStream_t st)
@@ -132,10 +229,22 @@ void launch_dot(const typename P::C* a, const typename P::C* b, long n, long str
   count_launch(), k_dot_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out);
 }
 
+template <class P>
+void launch_dot2(const typename P::C* a1, const typename P::C* b1, const typename P::C* a2,
+                 const typename P::C* b2, long n, long stride, int nslot, const int* sys_list, double2* partial,
+                 int nblk, double2* out1, double2* out2, cudaStream_t st)
+{
+  dim3 grd(nblk, nslot);
+  count_launch(), k_dot2_partial<P><<<grd, DOT_THREADS, 0, st>>>(a1, b1, a2, b2, n, stride, sys_list, partial, nblk);
+  count_launch(), k_dot2_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out1, out2);
+}
+
 template void launch_dot<F64>(const double2*, const double2*, long, long, int, const int*, double2*, int,
                               double2*, cudaStream_t);
 template void launch_dot<F32>(const float2*, const float2*, long, long, int, const int*, double2*, int,
                               double2*, cudaStream_t);
+template void launch_dot2<F32>(const float2*, const float2*, const float2*, const float2*, long, long, int,
+                               const int*, double2*, int, double2*, double2*, cudaStream_t);
 
 // ------------------------------------------------------------------ vector updates
 template <class P> __device__ __forceinline__ typename P::C cast_c(double2 v);
@@ -199,6 +308,21 @@ __global__ void k_vec_xr(long n, const int* __restrict__ sys_list, const KrylovS
   r[o] = csub<P>(s[o], cmul<P>(omega, t[o]));
 }
 
+// x += alpha pp + omega ss; r = s - omega t, with ss in a buffer of its own (the flexible
+// update of solver.c:153-156 when the preconditioned s is not kept in r)
+template <class P>
+__global__ void k_vec_xr_sep(long n, const int* __restrict__ sys_list, const KrylovScalars* __restrict__ ks,
+                             typename P::C* __restrict__ x, const typename P::C* __restrict__ pp,
+                             const typename P::C* __restrict__ ss, typename P::C* __restrict__ r,
+                             const typename P::C* __restrict__ s, const typename P::C* __restrict__ t)
+{
+  CSEM_VEC_PROLOGUE
+  if (ks[sys].status != ST_RUNNING) return;
+  const typename P::C alpha = cast_c<P>(ks[sys].alpha), omega = cast_c<P>(ks[sys].omega);
+  x[o] = cadd<P>(x[o], cadd<P>(cmul<P>(alpha, pp[o]), cmul<P>(omega, ss[o])));
+  r[o] = csub<P>(s[o], cmul<P>(omega, t[o]));
+}
+
 // p = r + beta (p - omega v)   (solver.c:166)
 template <class P>
 __global__ void k_vec_p(long n, const int* __restrict__ sys_list, const KrylovScalars* __restrict__ ks,
@@ -250,6 +374,15 @@ void launch_vec(int op, long n, int nslot, const int* sys_list, const KrylovScal
 }
 
 template <class P>
+void launch_vec_xr_sep(long n, int nslot, const int* sys_list, const KrylovScalars* ks, typename P::C* x,
+                       const typename P::C* pp, const typename P::C* ss, typename P::C* r,
+                       const typename P::C* s, const typename P::C* t, cudaStream_t st)
+{
+  dim3 grd((unsigned)((n + 255) / 256), nslot);
+  count_launch(), k_vec_xr_sep<P><<<grd, 256, 0, st>>>(n, sys_list, ks, x, pp, ss, r, s, t);
+}
+
+template <class P>
 void launch_axpy(long n, int nslot, const int* sys_list, const double2* coef, int coef_stride, int neg,
                  const typename P::C* x, typename P::C* y, cudaStream_t st)
 {
@@ -268,6 +401,8 @@ void launch_cdivv(long n, int nslot, const int* sys_list, const double2* d, int 
 #define CSEM_INST(P)                                                                                        \
   template void launch_vec<P>(int, long, int, const int*, const KrylovScalars*, P::C*, P::C*, P::C*, P::C*, \
                               P::C*, cudaStream_t);                                                         \
+  template void launch_vec_xr_sep<P>(long, int, const int*, const KrylovScalars*, P::C*, const P::C*,      \
+                                     const P::C*, P::C*, const P::C*, const P::C*, cudaStream_t);           \
   template void launch_axpy<P>(long, int, const int*, const double2*, int, int, const P::C*, P::C*,         \
                                cudaStream_t);                                                               \
   template void launch_cdivv<P>(long, int, const int*, const double2*, int, int, const P::C*, P::C*,        \

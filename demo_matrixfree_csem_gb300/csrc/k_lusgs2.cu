@@ -45,8 +45,10 @@ template <int VW> struct RegCap {
   static constexpr int value = VW == 1 ? CSEM_SWEEP_MAXNREG1 : (VW == 2 ? CSEM_SWEEP_MAXNREG2 : CSEM_SWEEP_MAXNREG4);
 };
 #define CSEM_SWEEP_BOUNDS(VW, MAXR) __launch_bounds__(MAXR) __maxnreg__(MAXR > NB_ROWS ? 128 : RegCap<VW>::value)
+#define CSEM_SWEEP_BOUNDS32(VW, MAXR) __launch_bounds__(MAXR) __maxnreg__(MAXR > NB_ROWS ? 128 : RegCap<VW>::value)
 #else
 #define CSEM_SWEEP_BOUNDS(VW, MAXR) __launch_bounds__(MAXR, MAXR > NB_ROWS ? 1 : MinBlocks<P, VW>::value)
+#define CSEM_SWEEP_BOUNDS32(VW, MAXR) __launch_bounds__(MAXR, MAXR > NB_ROWS ? 1 : MinBlocks<F32, VW>::value)
 #endif
 
 template <class P> struct View {
@@ -570,6 +572,355 @@ __global__ void CSEM_SWEEP_BOUNDS(VW, MAXR) k_sweep_eyz(SweepP<P> s)
   hand.finish(NC + R_ - 1);
 }
 
+// ---------------------------------------------------------------------------------------
+// complex64 sweeps: linear form, operands one step ahead.
+//
+// The update of a point is linear in the values it takes from the chain: its own row at
+// the previous march position (prev) and the previous row at this position (nb). With
+// the component's own point zero while its row is evaluated (fdfd.c:357,383,409), the
+// reference's update (b - aij) / aii rearranges to
+//   v = B + w (gp prev + gn nb),  w = iwmu / aii,
+//   B = b / (f aii) + w (known - cross),
+// where cross is the coupling to the other two components (read-only during the sweep),
+// known the own-component neighbours already fixed when the point is reached (the
+// not-yet-swept values of the backward sweep), gp and gn the spacing products of the two
+// chain neighbours and f = vol iom with fvm (1 otherwise). B, w, gp, gn depend only on
+// operands no other thread of the sweep writes before the point is reached, so each step
+// loads the next step's operands first, runs the short chain part (a real and a complex
+// multiply-add after nb arrives), hands over, and only then folds the loaded operands
+// into the next step's B and w while the loads were in flight. Same operations as the
+// reference up to the order of rounding (complex64 only; complex128 keeps the reference's
+// order in k_sweep_ex / k_sweep_eyz).
+namespace {
+
+struct Lin32 {
+  float2 B, w;
+  float gp, gn;
+};
+
+__device__ __forceinline__ float2 mul32(float2 a, float2 b)
+{
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 sub32(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 scl32(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+
+// the chain part: v = B + w (gp prev + gn nb)
+__device__ __forceinline__ float2 lin_apply(const Lin32& L, float2 prev, float2 nb)
+{
+  const float2 u = make_float2(L.gp * prev.x + L.gn * nb.x, L.gp * prev.y + L.gn * nb.y);
+  return make_float2(L.B.x + L.w.x * u.x - L.w.y * u.y, L.B.y + L.w.x * u.y + L.w.y * u.x);
+}
+
+// aii = gg iwmu - sg (fdfd.c fin); kc = known - cross
+__device__ __forceinline__ Lin32 lin_make(const SysScal<F32>& sc, int fvm, float gg, float sg, float vol,
+                                          float2 b, float2 kc, float gp, float gn)
+{
+  const float2 aii = make_float2(gg * sc.iwmu.x - sg, gg * sc.iwmu.y);
+  const float r = __frcp_rn(aii.x * aii.x + aii.y * aii.y);
+  const float2 inv = make_float2(aii.x * r, -aii.y * r);
+  Lin32 L;
+  L.w = mul32(sc.iwmu, inv);
+  float2 bt = mul32(b, inv);
+  if (fvm) {
+    const float2 f = make_float2(vol * sc.iom.x, vol * sc.iom.y);
+    const float rf = __frcp_rn(f.x * f.x + f.y * f.y);
+    bt = mul32(bt, make_float2(f.x * rf, -f.y * rf));
+  }
+  const float2 wk = mul32(L.w, kc);
+  L.B = make_float2(bt.x + wk.x, bt.y + wk.y);
+  L.gp = gp;
+  L.gn = gn;
+  return L;
+}
+
+// operands of one Ex step (the backward-only ones are dropped by the compiler forward)
+template <int VW> struct RawEx {
+  float2 b[VW], exjm[VW], exkm[VW], eyA[VW], eyB[VW], eyC[VW], eyD[VW], ezA[VW], ezB[VW], ezC[VW], ezD[VW];
+  float sg[VW];
+  Ax<F32> Y;
+};
+
+template <int VW> struct RawEyz {
+  float2 b[VW], xA[VW], xB[VW], xC[VW], xD[VW], yA[VW], yB[VW], yC[VW], yD[VW], own2[VW], rowold[VW];
+  float sg[VW];
+  Ax<F32> X[VW];
+};
+
+}  // namespace
+
+// Ex, complex64: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
+template <bool FWD, int VW, int MAXR>
+__global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
+{
+  typedef float2 C;
+  __shared__ HandOff<VW, C, (MAXR <= NB_ROWS)> hand;
+  const int slot = blockIdx.y;
+  const int sys = s.sys_list ? s.sys_list[slot] : slot;
+  const GridP<F32>& g = s.g;
+  const int n1 = g.n1, n2 = g.n2, nK = s.nK;
+  const int i0 = blockIdx.x * VW;
+  const View<F32> V = view_of<F32>(s, slot, sys);
+  const SysScal<F32> sc = s.scal[sys];
+  const C z = make_float2(0.f, 0.f);
+  const int R_ = nK - 1, M = n2 - 1;  // rows k = 1..R_, march j = 1..M
+  const int rr = threadIdx.x;
+  const bool rowok = rr < R_;
+  const int k = FWD ? 1 + rr : R_ - rr;
+  const Ax<F32> Z = rowok ? axis<F32>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<F32>{};
+  Ax<F32> X[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++)
+    X[q] = i0 + q < n1 ? axis_at<F32>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<F32>{};
+  C* ex0 = nullptr;
+  const C *ex1 = nullptr, *ey0 = nullptr, *ez0 = nullptr, *ez1 = nullptr, *bb = nullptr;
+  const float* sg0 = nullptr;
+  if (rowok) {
+    ex0 = V.row(0, k, 0) + i0;
+    ex1 = V.row(0, k - 1, 0) + i0;
+    ey0 = V.row(1, k, 0) + i0;
+    ez0 = V.row(2, k, 0) + i0;
+    ez1 = V.row(2, k - 1, 0) + i0;
+    bb = V.brow(0, k, 0);
+    if (bb) bb += i0;
+    sg0 = g.s11 + ix1(n1, n2, k, 0, i0);
+  }
+  const int L1 = n1 + 1;
+  const float gn = Z.r * (FWD ? Z.rsm : Z.rs);
+  RawEx<VW> raw;
+  Lin32 lin[VW];
+  // loads of march position c (nothing read here is written before that step)
+  auto load = [&](int c) {
+    const int j = FWD ? 1 + c : M - c;
+    raw.Y = axis<F32>(g.d2, g.d2s, g.r2, g.r2s, j);
+    const int ox = j * n1, oy = j * L1;
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      if (i0 + q < n1) {
+        raw.b[q] = bb ? ro(bb + ox + q) : z;
+        raw.sg[q] = ro(sg0 + ox + q);
+        if (!FWD) {
+          raw.exjm[q] = ex0[ox - n1 + q];
+          raw.exkm[q] = ex1[ox + q];
+          raw.eyA[q] = ro(ey0 + oy + q + 1);
+          raw.eyB[q] = ro(ey0 + oy + q);
+          raw.eyC[q] = ro(ey0 + oy - L1 + q + 1);
+          raw.eyD[q] = ro(ey0 + oy - L1 + q);
+          raw.ezA[q] = ro(ez0 + oy + q + 1);
+          raw.ezB[q] = ro(ez0 + oy + q);
+          raw.ezC[q] = ro(ez1 + oy + q + 1);
+          raw.ezD[q] = ro(ez1 + oy + q);
+        }
+      }
+    }
+  };
+  auto make = [&]() {
+    const Ax<F32>& Y = raw.Y;
+    const float gg = (Y.rs + Y.rsm) * Y.r + (Z.rs + Z.rsm) * Z.r;  // geo(Y, Z)
+    const float gp = Y.r * (FWD ? Y.rsm : Y.rs);
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      if (i0 + q >= n1) continue;
+      C kc = z;
+      if (!FWD) {
+        const C dy = sub32(sub32(raw.eyA[q], raw.eyB[q]), sub32(raw.eyC[q], raw.eyD[q]));
+        const C dz = sub32(sub32(raw.ezA[q], raw.ezB[q]), sub32(raw.ezC[q], raw.ezD[q]));
+        const C cross = scl32(X[q].rs, make_float2(Y.r * dy.x + Z.r * dz.x, Y.r * dy.y + Z.r * dz.y));
+        const C known = make_float2(Y.r * Y.rsm * raw.exjm[q].x + Z.r * Z.rsm * raw.exkm[q].x,
+                                    Y.r * Y.rsm * raw.exjm[q].y + Z.r * Z.rsm * raw.exkm[q].y);
+        kc = sub32(known, cross);
+      }
+      lin[q] = lin_make(sc, g.fvm, gg, raw.sg[q], X[q].ds * Y.d * Z.d, raw.b[q], kc, gp, gn);
+    }
+  };
+  C res[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) res[q] = z;
+  if (rowok && rr == 0 && M > 0) {
+    load(0);
+    make();
+  }
+  for (int T = 0; T < M + R_ - 1; T++) {
+    const int c = T - rr;
+    const bool act = rowok && c >= 0 && c < M;
+    const bool nxt = rowok && c + 1 >= 0 && c + 1 < M;
+    if (nxt) load(c + 1);
+    C nb[VW];
+    hand.get(res, nb, T);
+    if (act) {
+      const int ox = (FWD ? 1 + c : M - c) * n1;
+#pragma unroll
+      for (int q = 0; q < VW; q++) {
+        if (i0 + q >= n1) {
+          res[q] = z;
+          continue;
+        }
+        const C v = lin_apply(lin[q], res[q], nb[q]);  // prev: own row, previous j
+        ex0[ox + q] = v;
+        res[q] = v;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < VW; q++) res[q] = z;
+    }
+    hand.put(res, T);
+    if (nxt) make();
+  }
+  hand.finish(M + R_ - 1);
+}
+
+// Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j), complex64: march i in
+// chunks of VW. grid (lines, systems)
+template <int COMP, bool FWD, int VW, int MAXR>
+__global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
+{
+  typedef float2 C;
+  __shared__ HandOff<VW, C, (MAXR <= NB_ROWS)> hand;
+  const int slot = blockIdx.y;
+  const int sys = s.sys_list ? s.sys_list[slot] : slot;
+  const GridP<F32>& g = s.g;
+  const int n1 = g.n1, n2 = g.n2, nK = s.nK;
+  const int line = blockIdx.x;  // j (Ey) or k (Ez)
+  const View<F32> V = view_of<F32>(s, slot, sys);
+  const SysScal<F32> sc = s.scal[sys];
+  const C z = make_float2(0.f, 0.f);
+  const int R_ = COMP == 1 ? nK - 1 : n2 - 1;  // rows k (Ey) or j (Ez) = 1..R_
+  const int M = n1 - 1;                         // march i = 1..M
+  const int NC = (M + VW - 1) / VW;
+  const int rr = threadIdx.x;
+  const bool rowok = rr < R_;
+  const int r = FWD ? 1 + rr : R_ - rr;
+  const int k = COMP == 1 ? r : line;
+  const int j = COMP == 1 ? line : r;
+  // the line's and the row's spacings; R is the row axis (Z for Ey, Y for Ez), L the line's
+  Ax<F32> Y, Z;
+  if (COMP == 1) {
+    Y = axis_at<F32>(g.d2, g.d2s, g.r2, g.r2s, j);
+    Z = rowok ? axis<F32>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<F32>{};
+  } else {
+    Y = rowok ? axis<F32>(g.d2, g.d2s, g.r2, g.r2s, j) : Ax<F32>{};
+    Z = axis_at<F32>(g.d3, g.d3s, g.r3, g.r3s, k);
+  }
+  const Ax<F32>& Rw = COMP == 1 ? Z : Y;
+  C* own = nullptr;
+  const C *nxt = nullptr, *xa = nullptr, *xb = nullptr, *ya = nullptr, *yb = nullptr, *yc = nullptr, *yd = nullptr;
+  const C* bb = nullptr;
+  const float* sg0 = nullptr;
+  if (rowok) {
+    if (COMP == 1) {
+      own = V.row(1, k, j);
+      nxt = V.row(1, k - 1, j);
+      xa = V.row(0, k, j + 1);
+      xb = V.row(0, k, j);
+      ya = V.row(2, k, j + 1);
+      yb = V.row(2, k, j);
+      yc = V.row(2, k - 1, j + 1);
+      yd = V.row(2, k - 1, j);
+      sg0 = g.s22 + ix2(n1, n2, k, j, 0);
+    } else {
+      own = V.row(2, k, j);
+      nxt = V.row(2, k, j - 1);
+      xa = V.row(0, k + 1, j);
+      xb = V.row(0, k, j);
+      ya = V.row(1, k + 1, j);
+      yb = V.row(1, k, j);
+      yc = V.row(1, k + 1, j - 1);
+      yd = V.row(1, k, j - 1);
+      sg0 = g.s33 + ix3(n1, n2, k, j, 0);
+    }
+    bb = V.brow(COMP, k, j);
+  }
+  const float gn = Rw.r * (FWD ? Rw.rsm : Rw.rs);
+  // the coefficient of the line-axis differences in cross: Y.rs (Ey) or Z.rs (Ez)
+  const float lrs = COMP == 1 ? Y.rs : Z.rs;
+  RawEyz<VW> raw;
+  Lin32 lin[VW];
+  auto load = [&](int c) {
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      const int m = c * VW + q;
+      if (m < M) {
+        const int i = FWD ? 1 + m : M - m;
+        raw.X[q] = axis<F32>(g.d1, g.d1s, g.r1, g.r1s, i);
+        raw.b[q] = bb ? ro(bb + i) : z;
+        raw.sg[q] = ro(sg0 + i);
+        raw.xA[q] = ro(xa + i);
+        raw.xB[q] = ro(xb + i);
+        raw.xC[q] = ro(xa + i - 1);
+        raw.xD[q] = ro(xb + i - 1);
+        if (COMP == 2 || !FWD) {
+          raw.yA[q] = ro(ya + i);
+          raw.yB[q] = ro(yb + i);
+          raw.yC[q] = ro(yc + i);
+          raw.yD[q] = ro(yd + i);
+        }
+        if (!FWD) {
+          raw.own2[q] = own[i - 1];
+          raw.rowold[q] = nxt[i];
+        }
+      }
+    }
+  };
+  auto make = [&](int c) {
+#pragma unroll
+    for (int q = 0; q < VW; q++) {
+      if (c * VW + q >= M) continue;
+      const Ax<F32>& X = raw.X[q];
+      const float gg = (X.rs + X.rsm) * X.r + (Rw.rs + Rw.rsm) * Rw.r;  // geo(Z, X) / geo(X, Y)
+      const C dx = sub32(sub32(raw.xA[q], raw.xB[q]), sub32(raw.xC[q], raw.xD[q]));
+      // Ey: Y.rs (Z.r dEz + X.r dEx); Ez: Z.rs (X.r dEx + Y.r dEy)
+      C acc = scl32(X.r, dx);
+      if (COMP == 2 || !FWD) {
+        const C dy = sub32(sub32(raw.yA[q], raw.yB[q]), sub32(raw.yC[q], raw.yD[q]));
+        acc = make_float2(acc.x + Rw.r * dy.x, acc.y + Rw.r * dy.y);
+      }
+      C kc = scl32(-lrs, acc);
+      if (!FWD) {
+        const C known = make_float2(X.r * X.rsm * raw.own2[q].x + Rw.r * Rw.rsm * raw.rowold[q].x,
+                                    X.r * X.rsm * raw.own2[q].y + Rw.r * Rw.rsm * raw.rowold[q].y);
+        kc = make_float2(kc.x + known.x, kc.y + known.y);
+      }
+      lin[q] = lin_make(sc, g.fvm, gg, raw.sg[q], X.ds * Y.d * Z.d, raw.b[q], kc, X.r * (FWD ? X.rsm : X.rs), gn);
+    }
+  };
+  C res[VW];
+#pragma unroll
+  for (int q = 0; q < VW; q++) res[q] = z;
+  if (rowok && rr == 0 && NC > 0) {
+    load(0);
+    make(0);
+  }
+  for (int T = 0; T < NC + R_ - 1; T++) {
+    const int c = T - rr;
+    const bool act = rowok && c >= 0 && c < NC;
+    const bool nx = rowok && c + 1 >= 0 && c + 1 < NC;
+    if (nx) load(c + 1);
+    C nb[VW];
+    hand.get(res, nb, T);
+    if (act) {
+      C prev = c > 0 ? res[VW - 1] : z;  // own row at the previous march position
+#pragma unroll
+      for (int q = 0; q < VW; q++) {
+        const int m = c * VW + q;
+        if (m >= M) {
+          res[q] = z;
+          continue;
+        }
+        const C v = lin_apply(lin[q], prev, nb[q]);
+        own[FWD ? 1 + m : M - m] = v;
+        res[q] = v;
+        prev = v;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < VW; q++) res[q] = z;
+    }
+    hand.put(res, T);
+    if (nx) make(c + 1);
+  }
+  hand.finish(NC + R_ - 1);
+}
+
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
 {
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
@@ -582,6 +933,22 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
   const int threads = (rows + 31) / 32 * 32;
+  if constexpr (!P::exact) {
+    if (comp == 0) {
+      dim3 grd((n1 + VW - 1) / VW, nslot);
+      if (fwd) count_launch(), k_sweep_ex32<true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_ex32<false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    } else if (comp == 1) {
+      dim3 grd(n2, nslot);
+      if (fwd) count_launch(), k_sweep_eyz32<1, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_eyz32<1, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    } else {
+      dim3 grd(nK, nslot);
+      if (fwd) count_launch(), k_sweep_eyz32<2, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_eyz32<2, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    }
+    return;
+  }
   if (comp == 0) {
     dim3 grd((n1 + VW - 1) / VW, nslot);
     if (fwd) count_launch(), k_sweep_ex<P, true, VW, MAXR><<<grd, threads, 0, st>>>(s);

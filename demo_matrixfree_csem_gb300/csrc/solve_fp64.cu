@@ -80,6 +80,10 @@ void Solver64::M(int precond, int mp, const double2* x, double2* y)
 
 void Solver64::dot_async(const double2* a, const double2* b, int slot_out)
 {
+  if (seq_dots) {
+    launch_dot_seq(a, b, n, dots.as<double2>() + slot_out, st);
+    return;
+  }
   launch_dot<F64>(a, b, n, n, 1, nullptr, partial.as<double2>() + (size_t)slot_out * nblk, nblk,
                   dots.as<double2>() + slot_out, st);
 }

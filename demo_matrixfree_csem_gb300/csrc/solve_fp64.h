@@ -15,6 +15,9 @@ class Solver64 {
   int nblk;
   DevBuf scal, ks, dots, partial, coef, hist, work, prework;
   int nwork = 0, pre_mp = 0;
+  // dot products in the reference's sequential order (bit-identical to cdotprod.c)
+  // instead of the parallel tree; the context option "dot_order"
+  bool seq_dots = false;
   void set_iom(double re, double im);
   double2* W(int i);
   void ensure_work(int count);

@@ -61,12 +61,12 @@ MixedBatch::MixedBatch(Model* m_, int nsys_, cudaStream_t st_)
   b64.alloc(sizeof(double2) * N);
   r64.alloc(sizeof(double2) * N);
   w64.alloc(sizeof(double2) * N);
-  vec32.alloc(sizeof(float2) * N * 8);
+  vec32.alloc(sizeof(float2) * N * NVEC32);
   ks.alloc(sizeof(KrylovScalars) * nsys);
   sc64.alloc(sizeof(SysScal<F64>) * nsys);
   sc32.alloc(sizeof(SysScal<F32>) * nsys);
   dots.alloc(sizeof(double2) * 8 * nsys);
-  partial.alloc(sizeof(double2) * (size_t)nblk * nsys);
+  partial.alloc(sizeof(double2) * (size_t)nblk * nsys * 2);
   list.alloc(sizeof(int) * nsys);
   rn.alloc(sizeof(double) * nsys);
 }
@@ -142,28 +142,29 @@ void MixedBatch::inject(const float* src, const double* iom, int nch, const int*
 
 void MixedBatch::inner_iteration(int nact, const int* dl, int preco, int maxiter)
 {
-  float2 *r = V(0), *r0 = V(1), *p = V(2), *pp = V(3), *v = V(4), *s = V(5), *t = V(6), *d = V(7);
+  float2 *r = V(0), *r0 = V(1), *p = V(2), *pp = V(3), *v = V(4), *s = V(5), *t = V(6), *d = V(7), *sh = V(8);
   KrylovScalars* K = ks.as<KrylovScalars>();
   double2* D = dots.as<double2>();
   double2* part = partial.as<double2>();
   const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
+  // pp and sh are written only by the preconditioner, whose sweeps never write the
+  // boundary entries: zeroed once per solve, those stay zero, so the LU-SGS output is
+  // not cleared before each application
   auto M = [&](const float2* in, float2* out) {
     if (preco == PRE_APHI) o32.apply_aphi(in, out, nact, dl, sc);
-    else o32.apply_lusgs(in, out, nact, dl, sc);
+    else o32.apply_lusgs(in, out, nact, dl, sc, true);
   };
   M(p, pp);
   o32.apply_A(pp, v, nact, dl, sc);
   launch_dot<F32>(v, r0, n, n, nact, dl, part, nblk, D + 0 * nsys, st);
   launch_sc_alpha(nact, dl, K, D + 0 * nsys, st);
   launch_vec<F32>(VEC_S, n, nact, dl, K, r, v, s, nullptr, nullptr, st);
-  M(s, r);
-  o32.apply_A(r, t, nact, dl, sc);
-  launch_dot<F32>(s, t, n, n, nact, dl, part, nblk, D + 1 * nsys, st);
-  launch_dot<F32>(t, t, n, n, nact, dl, part, nblk, D + 2 * nsys, st);
+  M(s, sh);
+  o32.apply_A(sh, t, nact, dl, sc);
+  launch_dot2<F32>(s, t, t, t, n, n, nact, dl, part, nblk, D + 1 * nsys, D + 2 * nsys, st);
   launch_sc_omega(nact, dl, K, D + 1 * nsys, D + 2 * nsys, st);
-  launch_vec<F32>(VEC_XR, n, nact, dl, K, d, pp, r, s, t, st);
-  launch_dot<F32>(r, r, n, n, nact, dl, part, nblk, D + 3 * nsys, st);
-  launch_dot<F32>(r, r0, n, n, nact, dl, part, nblk, D + 4 * nsys, st);
+  launch_vec_xr_sep<F32>(n, nact, dl, K, d, pp, sh, r, s, t, st);
+  launch_dot2<F32>(r, r, r, r0, n, n, nact, dl, part, nblk, D + 3 * nsys, D + 4 * nsys, st);
   launch_sc_rs_beta(nact, dl, K, D + 3 * nsys, D + 4 * nsys, nullptr, 0, maxiter, st);
   launch_vec<F32>(VEC_P, n, nact, dl, K, r, p, v, nullptr, nullptr, st);
 }
@@ -188,8 +189,8 @@ void MixedBatch::start_inner(const std::vector<int>& g, const std::vector<double
   dim3 grd((unsigned)((n + 255) / 256), ng);
   count_launch(), k_start_inner<<<grd, 256, 0, st>>>(n, dl, rn.as<double>(), r64.as<double2>(), V(0), V(1), V(2), V(7));
   double2* D = dots.as<double2>();
-  launch_dot<F32>(V(0), V(1), n, n, ng, dl, partial.as<double2>(), nblk, D + 5 * nsys, st);
-  launch_dot<F32>(V(0), V(0), n, n, ng, dl, partial.as<double2>(), nblk, D + 6 * nsys, st);
+  launch_dot2<F32>(V(0), V(1), V(0), V(0), n, n, ng, dl, partial.as<double2>(), nblk, D + 5 * nsys, D + 6 * nsys,
+                   st);
   launch_sc_init(ng, dl, ks.as<KrylovScalars>(), D + 5 * nsys, D + 6 * nsys, nullptr, 0, st);
   CSEM_CUDA_TRY(cudaGetLastError());
 }
@@ -266,6 +267,7 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
   CSEM_CUDA_TRY(cudaMemsetAsync(x64.p, 0, sizeof(double2) * (size_t)nsys * n, st));
   CSEM_CUDA_TRY(cudaMemcpyAsync(r64.p, b64.p, sizeof(double2) * (size_t)nsys * n, cudaMemcpyDeviceToDevice, st));
   CSEM_CUDA_TRY(cudaMemsetAsync(ks.p, 0, sizeof(KrylovScalars) * nsys, st));
+  CSEM_CUDA_TRY(cudaMemsetAsync(vec32.p, 0, vec32.bytes, st));  // zero boundaries (inner_iteration)
   std::vector<int> all(nsys);
   for (int q = 0; q < nsys; q++) all[q] = q;
   std::vector<double> rnorm(nsys, 0.0), bn(nsys, 0.0);
@@ -367,9 +369,9 @@ void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double
   float2* GR0 = base + (size_t)(2 * m + 3) * N;
   const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
   double2* cf = gcoef.as<double2>();
-  auto M = [&](const float2* in, float2* out, int ng, const int* dl) {
+  auto M = [&](const float2* in, float2* out, int ng, const int* dl) {  // Z_j: only written here
     if (o.preco == PRE_APHI) o32.apply_aphi(in, out, ng, dl, sc);
-    else o32.apply_lusgs(in, out, ng, dl, sc);
+    else o32.apply_lusgs(in, out, ng, dl, sc, true);
   };
   // r0 = r64 / |r64|, d = 0 (k_start_inner writes r, r0, p, d: here r0 twice and d)
   {
@@ -500,6 +502,9 @@ void MixedBatch::solve_gmres(const std::vector<double>& bn, const double* tol, c
   const int m = std::max(1, o.nrestart);
   const size_t need = sizeof(float2) * (size_t)(2 * m + 4) * nsys * n;
   if (gm.bytes < need) gm.alloc(need);
+  // the Z_j are written only by the preconditioner, which leaves boundary entries as
+  // they are: they start at zero for this solve (the layout depends on m)
+  CSEM_CUDA_TRY(cudaMemsetAsync(gm.p, 0, need, st));
   const size_t needc = sizeof(double2) * (size_t)(m + 2) * nsys;
   if (gcoef.bytes < needc) gcoef.alloc(needc);
   const float2* GD = gm.as<float2>() + (size_t)(2 * m + 2) * nsys * n;

@@ -43,6 +43,8 @@ class MixedBatch {
   Ops<F32> o32;
   DevBuf x64, b64, r64, w64, vec32, ks, sc64, sc32, dots, partial, list, rn, srcbuf, chbuf, recbuf, outbuf;
   DevBuf gm, gcoef;  // GMRES basis (V, Z, w, d, r0) and per-system coefficients
+  // complex64 FBiCGStab vectors r, r0, p, pp, v, s, t, d (the correction), sh (preconditioned s)
+  static constexpr int NVEC32 = 9;
   float2* V(int i) { return vec32.as<float2>() + (size_t)i * nsys * n; }
   // b64 := injected sources (src [nsys][3], iom [nsys] on the host)
   void inject(const float* src, const double* iom, int nch, const int* ch);

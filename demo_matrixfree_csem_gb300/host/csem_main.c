@@ -12,7 +12,10 @@
  *             32  all (frequency x source) systems in one batched mixed-precision solve;
  *   nsrc=1|all    solve the first source row only (the reference, acq_init_free.c:56,90)
  *                 or every row, writing emf_NNNN.txt per source (NNNN = row number);
- *   inner_tol, check_every, max_outer   options of the mixed-precision solver.
+ *   inner_tol, check_every, max_outer   options of the mixed-precision solver;
+ *   fix_quirks=1  with airbc, inject the source with the conductivity of its own row
+ *                 (the reference reads it nb rows higher, inject_extract.c:55-63);
+ *   graphs=0|1, autotune=0|1   the context options of csem_ctx_set_option.
  */
 #include <math.h>
 #include <stdarg.h>
@@ -151,6 +154,13 @@ int main(int argc, char **argv)
   }
   csem_ctx *ctx;
   check(csem_ctx_create(&g, airbc, fvm, &ctx));
+  {
+    static const char *opt_keys[] = {"fix_quirks", "graphs", "autotune"};
+    for (int q = 0; q < 3; q++) {
+      int v;
+      if (csem_getparint(opt_keys[q], &v)) check(csem_ctx_set_option(ctx, opt_keys[q], v));
+    }
+  }
   long sz[10];
   csem_ctx_sizes(ctx, sz);
   const long lE = sz[0];

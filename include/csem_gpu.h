@@ -189,8 +189,8 @@ int csem_cdot_dev_noalloc(int prec, long n, int nsys, const void *a, const void 
 int csem_ctx_sync(csem_ctx *c);
 /* the context's CUDA stream (a cudaStream_t), for callers that record events on it */
 void *csem_ctx_stream(csem_ctx *c);
-/* Kernel-schedule options. complex128 results do not depend on them; complex64 results
- * may differ in the last bits between schedules:
+/* Kernel-schedule and solver options. complex128 results do not depend on the schedule
+ * options; complex64 results may differ in the last bits between schedules:
  *   "lusgs_pipelined" 1 (default): one launch per LU-SGS component sweep, rows as a
  *                     lockstep pipeline; 0: one launch per wavefront diagonal;
  *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
@@ -203,7 +203,18 @@ void *csem_ctx_stream(csem_ctx *c);
  *   "graphs"          1 (default): the batched BiCGStab replays the iterations between
  *                     two status reads as a captured CUDA graph (from the second time a
  *                     given number of systems is running; not while csem_profile is on);
- *                     0: direct launches.
+ *                     0: direct launches;
+ *   "dot_order"       complex128 solver only: 0 (default) dot products as a fixed
+ *                     parallel tree; 1 in the reference's sequential order (cdotprod.c:13-19),
+ *                     bit-identical to it, one dependent chain of additions per product,
+ *                     so the solve reproduces the reference's iterates bit for bit
+ *                     (without airbc; with airbc the FFT still differs in rounding) at
+ *                     a large cost in time;
+ *   "fix_quirks"      1: with airbc, source injection reads the conductivity at the
+ *                     source's own row of the air-included model; 0 (default): the
+ *                     reference's lookup after its -nb row shift (inject_extract.c:55-63,
+ *                     81-89), which reads nb rows higher and can land in the air. This
+ *                     option changes results (b, hence x and the receivers).
  */
 int csem_ctx_set_option(csem_ctx *c, const char *name, int value);
 

@@ -11,10 +11,19 @@
 # -Dmain=ref_main so the driver can also be called from the harness.
 # Flags follow the reference Makefile (-O3), plus -ffp-contract=off so that builds on
 # aarch64 (where GCC would otherwise fuse multiply-adds) match x86-64 bit for bit.
+# REF_VARIANT=fma builds instead into oracle/_ref_fma/ with multiply-add contraction
+# (-ffp-contract=fast, plus -mfma on x86-64): what the reference Makefile's flags give on
+# aarch64, used to measure how far the reference's own results move between builds.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${REF:-/root/reference}"
+CONTRACT="-ffp-contract=off"
 OUT="$HERE/_ref"
+if [ "${REF_VARIANT:-}" = "fma" ]; then
+  CONTRACT="-ffp-contract=fast"
+  if [ "$(uname -m)" = "x86_64" ]; then CONTRACT="$CONTRACT -mfma"; fi
+  OUT="$HERE/_ref_fma"
+fi
 OBJ="$OUT/obj"
 if [ ! -f "$REF/fdfd.c" ]; then
   echo "build_ref.sh: reference sources not found at $REF" >&2
@@ -22,7 +31,7 @@ if [ ! -f "$REF/fdfd.c" ]; then
 fi
 mkdir -p "$OBJ"
 CC="${CC:-gcc}"
-CFLAGS="-O3 -fPIC -ffp-contract=off -w -std=gnu99"
+CFLAGS="-O3 -fPIC $CONTRACT -w -std=gnu99"
 INC="-I$HERE/ref_stubs -I$REF"
 SRCS="cstd.c emf_init_free.c acq_init_free.c extend_model.c create_nugrid.c find_index.c \
       fdfd.c airbc_init_free.c inject_extract.c solver.c cdotprod.c gmres_init_free.c \

@@ -12,7 +12,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libcsemoracle.so")
-REF_LIB = os.path.join(HERE, "_ref", "libcsemref.so")
+# CSEM_REF_VARIANT=fma selects the multiply-add-contracting build (build_ref.sh)
+REF_VARIANT = os.environ.get("CSEM_REF_VARIANT", "")
+REF_LIB = os.path.join(HERE, "_ref_fma" if REF_VARIANT == "fma" else "_ref", "libcsemref.so")
 REF_SRC = os.environ.get("CSEM_REFERENCE_DIR", "/root/reference")
 
 _dp = C.POINTER(C.c_double)
@@ -44,7 +46,7 @@ def build_ref(force: bool = False) -> str | None:
         return REF_LIB if os.path.exists(REF_LIB) else None
     if force or not os.path.exists(REF_LIB):
         subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True,
-                       env=dict(os.environ, REF=REF_SRC), stdout=subprocess.DEVNULL)
+                       env=dict(os.environ, REF=REF_SRC, REF_VARIANT=REF_VARIANT), stdout=subprocess.DEVNULL)
     return REF_LIB
 
 

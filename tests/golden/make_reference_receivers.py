@@ -16,12 +16,19 @@ Output: tests/golden/<workload>/reference_receivers.npz (a few tens of KB).
 FFTW is replaced by the self-written DFT of oracle/fft2d.c (see oracle/ref_stubs), so
 the airwave part of these numbers carries that transform's rounding.
 
+With CSEM_REF_VARIANT=fma the reference is built with multiply-add contraction (what its
+Makefile's -O3 gives with GCC on aarch64, oracle/build_ref.sh) and the output is
+reference_receivers_fma.npz: the same solves from a second, equally valid build of the
+reference, which measures how far the reference's receivers move with rounding alone.
+
     python tests/golden/make_reference_receivers.py [layered_120|vti_block_120]
+    CSEM_REF_VARIANT=fma python tests/golden/make_reference_receivers.py vti_block_120
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -32,7 +39,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 def out_path(workload: str) -> str:
-    return os.path.join(HERE, workload, "reference_receivers.npz")
+    suffix = "_fma" if os.environ.get("CSEM_REF_VARIANT") == "fma" else ""
+    return os.path.join(HERE, workload, f"reference_receivers{suffix}.npz")
 
 
 def one(workload: str, ifreq: int, work: str) -> None:
@@ -66,7 +74,8 @@ def main() -> None:
     if not ref_available():
         sys.exit("reference sources not found")
     build_ref()
-    tmp = tempfile.mkdtemp()
+    os.makedirs(os.path.join(HERE, workload), exist_ok=True)
+    tmp = tempfile.mkdtemp(prefix="_work_", dir=os.path.join(HERE, workload))  # removed at the end
     works = [os.path.join(tmp, f"w{i}") for i in range(3)]
     for w in works:
         os.makedirs(w)
@@ -79,6 +88,7 @@ def main() -> None:
                         freqs=np.array([float(p["freq"]) for p in parts], np.float32),
                         hist0=parts[0]["hist"], hist1=parts[1]["hist"], hist2=parts[2]["hist"],
                         seconds=np.array([float(p["seconds"]) for p in parts]))
+    shutil.rmtree(tmp)
     print("wrote", OUT)
 
 

@@ -87,6 +87,31 @@ def test_short_solve_tracks_reference(gpu, case):
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_reference_order_dots_reproduce_reference_solve(gpu, case):
+    """dot_order=1: dot products in the reference's sequential order. Then the complex128
+    solve repeats the reference's arithmetic: without airbc its iterate is the reference's
+    (the fixture's x_solve) bit for bit, and its residual history and iteration count are
+    the oracle's exactly; with airbc only the airwave FFT's rounding differs (cuFFT
+    against the DFT the oracle and the fixtures use), bounded as the short solves above."""
+    d, p, gold, G, ctx = _ctx(case)
+    ctx.set_option("dot_order", 1)
+    iom = cs.iom_of(gold["freqs"][0])
+    b = gold["b"]
+    kw = dict(algopt=int(p["algopt"]), niter=int(p["niter"]), tol=tol_of(p, 0, gold["freqs"]),
+              nrestart=int(p.get("nrestart", 10)), mp=int(p.get("mp", 30)))
+    x, hist, it, st = ctx.solve_fp64(iom, b, preco=int(p["preco"]), **kw)
+    O = oracle_for(G, p)
+    O.set_freq(float(gold["freqs"][0]))
+    x0, h0, it0 = O.solve(b, precond=int(p["preco"]), **kw)
+    if int(p.get("airbc", 0)) == 0:
+        assert np.array_equal(x, gold["x_solve"])
+        assert it == it0 and np.array_equal(hist[:len(h0)], h0), (it, it0)
+    else:
+        x1, _, _ = O.solve(b * (1 + 2.0 ** -52), precond=int(p["preco"]), **kw)
+        assert relerr(x, gold["x_solve"]) <= max(1e-9, 100 * relerr(x1, x0))
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_c64_operators_close_to_fp64(gpu, case):
     d, p, gold, G, ctx = _ctx(case)
     iom = cs.iom_of(gold["freqs"][0])

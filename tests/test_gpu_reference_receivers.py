@@ -8,11 +8,18 @@ relative per frequency and channel. Ey is zero by symmetry on the receiver line 
 values are rounding noise, about 1e-8 of Ex), so Ey is measured against the Ex max.
 
 Bounds:
-  * complex128 GPU drop-in (injection, solve, extraction through the C ABI): Ex, Ez
-    <= 5e-9 (the two runs differ only in dot-product summation order and in the
-    airwave FFT's rounding, which BiCGStab amplifies over hundreds of iterations);
-    iteration counts within 15%; the first 10 residuals within 2e-6 relative (the reference prints 7 digits;
-    the two histories separate after 13-25 iterations as rounding differences grow);
+  * complex128 GPU drop-in (injection, solve, extraction through the C ABI), per
+    frequency: max(1e-9, 5 x the reference's own spread), where the spread is how far the
+    reference's receivers move between two valid builds of it: reference_receivers_fma.npz
+    holds the same solves from the reference built with multiply-add contraction (what
+    its Makefile's -O3 gives with GCC on aarch64). The GPU run differs from the reference
+    only in the dot products' summation order and the airwave FFT's rounding, which
+    BiCGStab amplifies over hundreds of iterations just as contraction does: at 0.25 Hz
+    the reference moves by 6e-10 (layered) and 1.0e-8 (VTI) between its own builds.
+    Iteration counts within 20% (the two reference builds differ by up to 16%); the first
+    10 residuals within 2e-6 relative (the reference prints 7 digits);
+  * complex128 with dot_order=1 (the reference's summation order), at the highest
+    frequency: <= 1e-9, the only remaining difference being the FFT's rounding;
   * batched mixed precision (complex64 inner, complex128 defect correction): <= 1e-7.
 """
 import os
@@ -38,7 +45,10 @@ def layered(request, tmp_path_factory):
     synthetic.write_config(cfg, d)
     p = {k: str(v) for k, v in cfg.params.items()}
     G = product_grid(d, p)
-    return cfg, cs.Ctx(G, 1, 0), np.load(os.path.join(GOLDEN, request.param, "reference_receivers.npz"))
+    z = dict(np.load(os.path.join(GOLDEN, request.param, "reference_receivers.npz")))
+    fma = np.load(os.path.join(GOLDEN, request.param, "reference_receivers_fma.npz"))
+    z["spread"] = np.array([max(_errors(fma["rec"][f], z["rec"][f])) for f in range(len(z["freqs"]))])
+    return cfg, cs.Ctx(G, 1, 0), z
 
 
 def _errors(dcal, ref):
@@ -57,10 +67,27 @@ def test_fp64_dropin_matches_reference(gpu, layered):
         x, hist, it, st = ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=1000, tol=tol)
         assert st == "converged"
         err = _errors(ctx.extract_emf(["Ex", "Ey", "Ez"], cfg.acq.rec, x), z["rec"][f])
-        assert max(err) <= 5e-9, (freq, err)
+        assert max(err) <= max(1e-9, 5 * z["spread"][f]), (freq, err, z["spread"][f])
         href = z[f"hist{f}"]
-        assert abs(it - (len(href) - 1)) <= 0.15 * (len(href) - 1), (freq, it, len(href) - 1)
+        assert abs(it - (len(href) - 1)) <= 0.2 * (len(href) - 1), (freq, it, len(href) - 1)
         np.testing.assert_allclose(hist[:10], href[:10], rtol=2e-6)
+
+
+def test_fp64_reference_dot_order_within_1e9(gpu, layered):
+    cfg, ctx, z = layered
+    f = len(z["freqs"]) - 1
+    freq = float(z["freqs"][f])
+    iom = cs.iom_of(freq)
+    b = ctx.inject_source(iom, ["Ex"], cfg.acq.src[0])
+    tol = float(np.float32(np.float32(1e-8) / np.float32(freq)))
+    ctx.set_option("dot_order", 1)
+    try:
+        x, hist, it, st = ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=1000, tol=tol)
+    finally:
+        ctx.set_option("dot_order", 0)
+    assert st == "converged"
+    err = _errors(ctx.extract_emf(["Ex", "Ey", "Ez"], cfg.acq.rec, x), z["rec"][f])
+    assert max(err) <= 1e-9, (freq, err)
 
 
 def test_mixed_batch_matches_reference(gpu, layered):
