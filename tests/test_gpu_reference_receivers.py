@@ -19,7 +19,8 @@ Bounds:
     Iteration counts within 20% (the two reference builds differ by up to 16%); the first
     10 residuals within 2e-6 relative (the reference prints 7 digits);
   * complex128 with dot_order=1 (the reference's summation order), at the highest
-    frequency: <= 1e-9, the only remaining difference being the FFT's rounding;
+    frequency: <= 1e-9, the only remaining difference being the FFT's rounding (slow:
+    run with CSEM_SLOW_TESTS=1);
   * batched mixed precision (complex64 inner, complex128 defect correction): <= 1e-7.
 """
 import os
@@ -73,7 +74,10 @@ def test_fp64_dropin_matches_reference(gpu, layered):
         np.testing.assert_allclose(hist[:10], href[:10], rtol=2e-6)
 
 
+@pytest.mark.skipif(os.environ.get("CSEM_SLOW_TESTS") != "1",
+                    reason="the reference's sequential dot order takes minutes here; CSEM_SLOW_TESTS=1 runs it")
 def test_fp64_reference_dot_order_within_1e9(gpu, layered):
+    """About 0.2 s per sequential dot product on 4.8M unknowns, 5 per iteration."""
     cfg, ctx, z = layered
     f = len(z["freqs"]) - 1
     freq = float(z["freqs"][f])
@@ -87,6 +91,7 @@ def test_fp64_reference_dot_order_within_1e9(gpu, layered):
         ctx.set_option("dot_order", 0)
     assert st == "converged"
     err = _errors(ctx.extract_emf(["Ex", "Ey", "Ez"], cfg.acq.rec, x), z["rec"][f])
+    print(f"dot_order=1 {freq} Hz: errors {err}, iterations {it} (reference {len(z[f'hist{f}']) - 1})")
     assert max(err) <= 1e-9, (freq, err)
 
 
