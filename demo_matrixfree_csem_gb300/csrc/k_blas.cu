@@ -50,6 +50,11 @@ struct Acc2 {  // compensated float accumulator for one real component
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// a per-system double2 scalar in the vector's precision
+template <class P> __device__ __forceinline__ typename P::C cast_c(double2 v);
+template <> __device__ __forceinline__ double2 cast_c<F64>(double2 v) { return v; }
+template <> __device__ __forceinline__ float2 cast_c<F32>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
 __device__ __forceinline__ double2 warp_sum(double2 v)
 {
   for (int o = 16; o > 0; o >>= 1) {
@@ -181,7 +186,7 @@ __global__ void k_dot2_final(const double2* __restrict__ partial, int nblk, doub
 // reference's bit for bit. The sum is one dependent chain per component: thread 0 adds
 // a chunk of products from shared memory while the other threads form the next chunk's
 // products (coalesced loads), one CTA per call.
-static constexpr int SEQ_CHUNK = 2048;
+static constexpr int SEQ_CHUNK = 1024;  // 2 x 16 KB of products
 
 __global__ void __launch_bounds__(DOT_THREADS)
 k_dot_seq(const double2* __restrict__ a, const double2* __restrict__ b, long n, double2* __restrict__ out)
@@ -220,6 +225,58 @@ void launch_dot_seq(const double2* a, const double2* b, long n, double2* out, cu
   count_launch(), k_dot_seq<<<1, DOT_THREADS, 0, st>>>(a, b, n, out);
 }
 
+// The flexible BiCGStab update with its two dot products in one pass (solver.c:153-156,
+// 157-160): x += alpha pp + omega ss, r = s - omega t (ss in a buffer of its own), then
+// r.conj(r) and r.conj(r0). The pass walks the dot products' partition in their
+// per-thread order, so both values equal those of k_dot2_partial on the updated r bit for
+// bit; systems no longer running keep x and r and still get their dot products.
+template <class P>
+__global__ void __launch_bounds__(DOT_THREADS)
+k_xr_dot2(long n, const int* __restrict__ sys_list, const KrylovScalars* __restrict__ ks,
+          typename P::C* __restrict__ x, const typename P::C* __restrict__ pp, const typename P::C* __restrict__ ss,
+          typename P::C* __restrict__ r, const typename P::C* __restrict__ s, const typename P::C* __restrict__ t,
+          const typename P::C* __restrict__ r0, double2* __restrict__ partial, int nblk)
+{
+  typedef typename P::C C;
+  const int slot = blockIdx.y;
+  const int sys = sys_list ? sys_list[slot] : slot;
+  const size_t so = (size_t)sys * n;
+  const long chunk = (n + nblk - 1) / nblk;
+  const long beg = (long)blockIdx.x * chunk, end = min(n, beg + chunk);
+  const bool run = ks[sys].status == ST_RUNNING;
+  const C alpha = cast_c<P>(ks[sys].alpha), omega = cast_c<P>(ks[sys].omega);
+  DotAcc<P> d1, d2;
+  for (long q = beg + threadIdx.x; q < end; q += DOT_THREADS) {
+    C rv;
+    if (run) {
+      x[so + q] = cadd<P>(x[so + q], cadd<P>(cmul<P>(alpha, pp[so + q]), cmul<P>(omega, ss[so + q])));
+      rv = csub<P>(s[so + q], cmul<P>(omega, t[so + q]));
+      r[so + q] = rv;
+    } else {
+      rv = r[so + q];
+    }
+    d1.add(rv, rv);
+    d2.add(rv, r0[so + q]);
+  }
+  const double2 acc1 = block_sum(d1.value());
+  const double2 acc2 = block_sum(d2.value());
+  if (threadIdx.x == 0) {
+    partial[(size_t)slot * nblk + blockIdx.x] = acc1;
+    partial[(size_t)(gridDim.y + slot) * nblk + blockIdx.x] = acc2;
+  }
+}
+
+template <class P>
+void launch_xr_dot2(long n, int nslot, const int* sys_list, const KrylovScalars* ks, typename P::C* x,
+                    const typename P::C* pp, const typename P::C* ss, typename P::C* r, const typename P::C* s,
+                    const typename P::C* t, const typename P::C* r0, double2* partial, int nblk, double2* out_rr,
+                    double2* out_rr0, cudaStream_t st)
+{
+  dim3 grd(nblk, nslot);
+  count_launch(), k_xr_dot2<P><<<grd, DOT_THREADS, 0, st>>>(n, sys_list, ks, x, pp, ss, r, s, t, r0, partial, nblk);
+  count_launch(), k_dot2_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out_rr, out_rr0);
+}
+
 template <class P>
 void launch_dot(const typename P::C* a, const typename P::C* b, long n, long stride, int nslot,
                 const int* sys_list, double2* partial, int nblk, double2* out, cudaStream_t st)
@@ -245,11 +302,11 @@ template void launch_dot<F32>(const float2*, const float2*, long, long, int, con
                               double2*, cudaStream_t);
 template void launch_dot2<F32>(const float2*, const float2*, const float2*, const float2*, long, long, int,
                                const int*, double2*, int, double2*, double2*, cudaStream_t);
+template void launch_xr_dot2<F32>(long, int, const int*, const KrylovScalars*, float2*, const float2*,
+                                  const float2*, float2*, const float2*, const float2*, const float2*, double2*, int,
+                                  double2*, double2*, cudaStream_t);
 
 // ------------------------------------------------------------------ vector updates
-template <class P> __device__ __forceinline__ typename P::C cast_c(double2 v);
-template <> __device__ __forceinline__ double2 cast_c<F64>(double2 v) { return v; }
-template <> __device__ __forceinline__ float2 cast_c<F32>(double2 v) { return make_float2((float)v.x, (float)v.y); }
 
 #define CSEM_VEC_PROLOGUE                                                  \
   const int slot = blockIdx.y;                                             \
@@ -308,21 +365,6 @@ __global__ void k_vec_xr(long n, const int* __restrict__ sys_list, const KrylovS
   r[o] = csub<P>(s[o], cmul<P>(omega, t[o]));
 }
 
-// x += alpha pp + omega ss; r = s - omega t, with ss in a buffer of its own (the flexible
-// update of solver.c:153-156 when the preconditioned s is not kept in r)
-template <class P>
-__global__ void k_vec_xr_sep(long n, const int* __restrict__ sys_list, const KrylovScalars* __restrict__ ks,
-                             typename P::C* __restrict__ x, const typename P::C* __restrict__ pp,
-                             const typename P::C* __restrict__ ss, typename P::C* __restrict__ r,
-                             const typename P::C* __restrict__ s, const typename P::C* __restrict__ t)
-{
-  CSEM_VEC_PROLOGUE
-  if (ks[sys].status != ST_RUNNING) return;
-  const typename P::C alpha = cast_c<P>(ks[sys].alpha), omega = cast_c<P>(ks[sys].omega);
-  x[o] = cadd<P>(x[o], cadd<P>(cmul<P>(alpha, pp[o]), cmul<P>(omega, ss[o])));
-  r[o] = csub<P>(s[o], cmul<P>(omega, t[o]));
-}
-
 // p = r + beta (p - omega v)   (solver.c:166)
 template <class P>
 __global__ void k_vec_p(long n, const int* __restrict__ sys_list, const KrylovScalars* __restrict__ ks,
@@ -374,15 +416,6 @@ void launch_vec(int op, long n, int nslot, const int* sys_list, const KrylovScal
 }
 
 template <class P>
-void launch_vec_xr_sep(long n, int nslot, const int* sys_list, const KrylovScalars* ks, typename P::C* x,
-                       const typename P::C* pp, const typename P::C* ss, typename P::C* r,
-                       const typename P::C* s, const typename P::C* t, cudaStream_t st)
-{
-  dim3 grd((unsigned)((n + 255) / 256), nslot);
-  count_launch(), k_vec_xr_sep<P><<<grd, 256, 0, st>>>(n, sys_list, ks, x, pp, ss, r, s, t);
-}
-
-template <class P>
 void launch_axpy(long n, int nslot, const int* sys_list, const double2* coef, int coef_stride, int neg,
                  const typename P::C* x, typename P::C* y, cudaStream_t st)
 {
@@ -401,8 +434,6 @@ void launch_cdivv(long n, int nslot, const int* sys_list, const double2* d, int 
 #define CSEM_INST(P)                                                                                        \
   template void launch_vec<P>(int, long, int, const int*, const KrylovScalars*, P::C*, P::C*, P::C*, P::C*, \
                               P::C*, cudaStream_t);                                                         \
-  template void launch_vec_xr_sep<P>(long, int, const int*, const KrylovScalars*, P::C*, const P::C*,      \
-                                     const P::C*, P::C*, const P::C*, const P::C*, cudaStream_t);           \
   template void launch_axpy<P>(long, int, const int*, const double2*, int, int, const P::C*, P::C*,         \
                                cudaStream_t);                                                               \
   template void launch_cdivv<P>(long, int, const int*, const double2*, int, int, const P::C*, P::C*,        \

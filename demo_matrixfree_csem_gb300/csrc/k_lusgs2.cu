@@ -12,18 +12,17 @@
 // position T - t, so the row before it finished that position at step T - 1. That value
 // arrives by warp shuffle, or through shared memory from the last lane of the previous
 // warp (pairwise named barriers between neighbouring warps). The own-row dependency stays
-// in registers and the
-// sweep's first row depends on the boundary, which is zero. A sweep takes
-// (march positions + rows - 1) steps.
+// in registers and the sweep's first row depends on the boundary, which is zero. A sweep
+// takes (march positions + rows - 1) steps.
 //
 // Inside a step a thread first issues every load it needs for its VW points (none of
 // them is written in this step), then computes and stores, so one memory round trip
 // is exposed per step instead of one per point.
 //
-// Every point is evaluated with the same operations, operands and order as the
-// reference (the F64 instantiation is bit-identical to it and to the one-launch-per-
-// diagonal kernels of k_lusgs.cu); F32 uses reciprocal spacings and a reciprocal-based
-// complex quotient.
+// In k_sweep_ex / k_sweep_eyz every point is evaluated with the same operations, operands
+// and order as the reference (the complex128 instantiation is bit-identical to it and to
+// the one-launch-per-diagonal kernels of k_lusgs.cu). complex64 runs k_sweep_ex32 /
+// k_sweep_eyz32 below: the same update in linear form, with reciprocal spacings.
 #include "csem_cuda.cuh"
 #include "engine.h"
 
@@ -933,7 +932,7 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
   const int threads = (rows + 31) / 32 * 32;
-  if constexpr (!P::exact) {
+  if constexpr (!P::exact) {  // complex64: the linear-form sweeps
     if (comp == 0) {
       dim3 grd((n1 + VW - 1) / VW, nslot);
       if (fwd) count_launch(), k_sweep_ex32<true, VW, MAXR><<<grd, threads, 0, st>>>(s);
@@ -947,20 +946,20 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
       if (fwd) count_launch(), k_sweep_eyz32<2, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
       else count_launch(), k_sweep_eyz32<2, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
     }
-    return;
-  }
-  if (comp == 0) {
-    dim3 grd((n1 + VW - 1) / VW, nslot);
-    if (fwd) count_launch(), k_sweep_ex<P, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
-    else count_launch(), k_sweep_ex<P, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
-  } else if (comp == 1) {
-    dim3 grd(n2, nslot);
-    if (fwd) count_launch(), k_sweep_eyz<P, 1, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
-    else count_launch(), k_sweep_eyz<P, 1, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
-  } else {
-    dim3 grd(nK, nslot);
-    if (fwd) count_launch(), k_sweep_eyz<P, 2, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
-    else count_launch(), k_sweep_eyz<P, 2, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+  } else {  // complex128: the reference's operation order
+    if (comp == 0) {
+      dim3 grd((n1 + VW - 1) / VW, nslot);
+      if (fwd) count_launch(), k_sweep_ex<P, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_ex<P, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    } else if (comp == 1) {
+      dim3 grd(n2, nslot);
+      if (fwd) count_launch(), k_sweep_eyz<P, 1, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_eyz<P, 1, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    } else {
+      dim3 grd(nK, nslot);
+      if (fwd) count_launch(), k_sweep_eyz<P, 2, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_eyz<P, 2, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+    }
   }
 }
 

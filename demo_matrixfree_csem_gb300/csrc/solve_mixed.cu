@@ -163,8 +163,7 @@ void MixedBatch::inner_iteration(int nact, const int* dl, int preco, int maxiter
   o32.apply_A(sh, t, nact, dl, sc);
   launch_dot2<F32>(s, t, t, t, n, n, nact, dl, part, nblk, D + 1 * nsys, D + 2 * nsys, st);
   launch_sc_omega(nact, dl, K, D + 1 * nsys, D + 2 * nsys, st);
-  launch_vec_xr_sep<F32>(n, nact, dl, K, d, pp, sh, r, s, t, st);
-  launch_dot2<F32>(r, r, r, r0, n, n, nact, dl, part, nblk, D + 3 * nsys, D + 4 * nsys, st);
+  launch_xr_dot2<F32>(n, nact, dl, K, d, pp, sh, r, s, t, r0, part, nblk, D + 3 * nsys, D + 4 * nsys, st);
   launch_sc_rs_beta(nact, dl, K, D + 3 * nsys, D + 4 * nsys, nullptr, 0, maxiter, st);
   launch_vec<F32>(VEC_P, n, nact, dl, K, r, p, v, nullptr, nullptr, st);
 }

@@ -25,10 +25,11 @@ enum VecOp { VEC_INIT = 0, VEC_S = 1, VEC_XR = 2, VEC_P = 3, VEC_XR_PLAIN = 4, V
 template <class P>
 void launch_vec(int op, long n, int nslot, const int* sys_list, const KrylovScalars* ks, typename P::C* a,
                 typename P::C* b, typename P::C* c, typename P::C* d, typename P::C* e, cudaStream_t st);
-template <class P>  // x += alpha pp + omega ss; r = s - omega t (ss apart from r)
-void launch_vec_xr_sep(long n, int nslot, const int* sys_list, const KrylovScalars* ks, typename P::C* x,
-                       const typename P::C* pp, const typename P::C* ss, typename P::C* r,
-                       const typename P::C* s, const typename P::C* t, cudaStream_t st);
+template <class P>  // x += alpha pp + omega ss; r = s - omega t (ss apart from r); r.r, r.r0
+void launch_xr_dot2(long n, int nslot, const int* sys_list, const KrylovScalars* ks, typename P::C* x,
+                    const typename P::C* pp, const typename P::C* ss, typename P::C* r, const typename P::C* s,
+                    const typename P::C* t, const typename P::C* r0, double2* partial, int nblk, double2* out_rr,
+                    double2* out_rr0, cudaStream_t st);
 template <class P>
 void launch_axpy(long n, int nslot, const int* sys_list, const double2* coef, int coef_stride, int neg,
                  const typename P::C* x, typename P::C* y, cudaStream_t st);

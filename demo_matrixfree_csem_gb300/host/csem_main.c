@@ -15,6 +15,8 @@
  *   inner_tol, check_every, max_outer   options of the mixed-precision solver;
  *   fix_quirks=1  with airbc, inject the source with the conductivity of its own row
  *                 (the reference reads it nb rows higher, inject_extract.c:55-63);
+ *   dot_order=1   complex128 dot products in the reference's sequential order (its
+ *                 iterates bit for bit, slowly);
  *   graphs=0|1, autotune=0|1   the context options of csem_ctx_set_option.
  */
 #include <math.h>
@@ -155,8 +157,8 @@ int main(int argc, char **argv)
   csem_ctx *ctx;
   check(csem_ctx_create(&g, airbc, fvm, &ctx));
   {
-    static const char *opt_keys[] = {"fix_quirks", "graphs", "autotune"};
-    for (int q = 0; q < 3; q++) {
+    static const char *opt_keys[] = {"fix_quirks", "dot_order", "graphs", "autotune"};
+    for (int q = 0; q < 4; q++) {
       int v;
       if (csem_getparint(opt_keys[q], &v)) check(csem_ctx_set_option(ctx, opt_keys[q], v));
     }
