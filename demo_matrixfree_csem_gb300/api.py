@@ -341,7 +341,7 @@ class _BatchOpts(C.Structure):
 
 
 def solve_batch(ctx: Ctx, freqs, srcs, chsrc=("Ex",), chrec=("Ex", "Ey", "Ez"), rec=None, precision=32, algopt=1,
-                preco=1, niter=1000, tol=1e-8, inner_tol=0.1, check_every=4, max_outer=30, nrestart=10, mp=30):
+                preco=1, niter=1000, tol=1e-8, inner_tol=0.2, check_every=4, max_outer=30, nrestart=10, mp=30):
     """Solve len(freqs) systems (frequency freqs[s], dipole at srcs[s]) and extract the
     receivers rec ([nrec][5] rows). Returns a dict with dcal [nsys][nchrec][nrec]
     (complex128), iters, outer, status, relres."""
@@ -384,7 +384,7 @@ def solve_batches(jobs):
         chsrc = j.pop("chsrc", ("Ex",))
         chrec = j.pop("chrec", ("Ex", "Ey", "Ez"))
         rec = j.pop("rec", None)
-        d = dict(precision=32, algopt=1, preco=1, niter=1000, tol=1e-8, inner_tol=0.1, check_every=4, max_outer=30,
+        d = dict(precision=32, algopt=1, preco=1, niter=1000, tol=1e-8, inner_tol=0.2, check_every=4, max_outer=30,
                  nrestart=10, mp=30)
         d.update(j)
         o = _BatchOpts(d["precision"], d["algopt"], d["preco"], d["niter"], d["tol"], d["inner_tol"],

@@ -534,7 +534,7 @@ int csem_solve_batch_host(csem_ctx* c, int nsys, const float* freq, const float*
     mo.max_inner_total = 3 * mo.niter;
     mo.max_outer = opt->max_outer > 0 ? opt->max_outer : 30;
     mo.preco = opt->preco;
-    mo.inner_tol = opt->inner_tol > 0 ? opt->inner_tol : 0.1;
+    mo.inner_tol = opt->inner_tol > 0 ? opt->inner_tol : 0.2;
     mo.check_every = opt->check_every > 0 ? opt->check_every : 4;
     mo.autotune = c->autotune;
     mo.algopt = opt->algopt;

@@ -13,7 +13,7 @@ struct MixedOptions {
   int max_inner_total = 3000;
   int max_outer = 30;
   int preco = 1;            // 1 LU-SGS, 3 A-phi
-  double inner_tol = 0.1;   // relative reduction asked of one inner solve
+  double inner_tol = 0.2;   // relative reduction asked of one inner solve
   int check_every = 4;      // inner iterations between host status reads
   bool autotune = false;    // time the LU-SGS sweep variants on the batch, keep the fastest
   int algopt = 1;           // inner solver: 1 flexible BiCGStab, 2 flexible GMRES(nrestart)

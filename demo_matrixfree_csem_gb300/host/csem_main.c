@@ -113,7 +113,7 @@ int main(int argc, char **argv)
   if (!csem_getparint("param_extended", &param_extended)) param_extended = 0;
   if (!csem_getparint("n1fft", &n1fft)) n1fft = 1024;
   if (!csem_getparint("n2fft", &n2fft)) n2fft = 1024;
-  if (!csem_getpardouble("inner_tol", &inner_tol)) inner_tol = 0.1;
+  if (!csem_getpardouble("inner_tol", &inner_tol)) inner_tol = 0.2;
   if (!csem_getparint("check_every", &check_every)) check_every = 4;
   if (!csem_getparint("max_outer", &max_outer)) max_outer = 30;
   char *nsrc_s = NULL;

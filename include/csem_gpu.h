@@ -116,7 +116,7 @@ typedef struct csem_batch_opts {
   int preco;         /* 0 none, 1 LU-SGS, 2 inner GMRES (64 only), 3 A-phi */
   int niter;         /* the reference's niter */
   float tol;         /* the reference's tol; system s stops at tol/freq[s] in float (main.c:94) */
-  double inner_tol;  /* precision 32: relative reduction of one inner solve (<= 0: 0.1) */
+  double inner_tol;  /* precision 32: relative reduction of one inner solve (<= 0: 0.2) */
   int check_every;   /* precision 32: inner iterations between status reads (<= 0: 4) */
   int max_outer;     /* precision 32: defect-correction cycles (<= 0: 30) */
   int nrestart, mp;  /* GMRES(nrestart); precision 64: GMRES(mp) preconditioner */
@@ -157,7 +157,9 @@ int csem_solve_batches_host(int njobs, csem_batch_job *jobs);
  * needs for nsys systems with this precision and preconditioner, beyond the model and
  * cuFFT's work areas. csem_batch_capacity: the largest nsys whose batch fits in
  * budget_bytes (precision 64 solves one system at a time: any count if one fits, else 0).
- * Callers with more systems solve them in waves of that size. */
+ * Callers with more systems solve them in waves of that size. Both count the mixed path's
+ * BiCGStab inner solver (algopt 1); its GMRES inner solver (algopt 2) needs
+ * (2 nrestart + 4) x 8 bytes more per unknown and system, for its basis. */
 int csem_batch_bytes(csem_ctx *c, int precision, int preco, int nsys, double *bytes);
 int csem_batch_capacity(csem_ctx *c, int precision, int preco, double budget_bytes, int *nsys);
 
