@@ -221,12 +221,11 @@ int main(int argc, char **argv)
         check(csem_solve_fp64_host(ctx, algopt, preco, niter, tolf, nrestart, mp, 0.0, iom_im, b, x, hist, hcap, &nh,
                                    &iters, &status));
         double t1 = now();
-        if (verb) {
+        if (verb && status != CSEM_ST_ZERO_RHS) {
           FILE *fp = fopen(hist_name(algopt, preco), "w");
           if (fp) {
             fprintf(fp, algopt == 1 ? "iteration \t relres\n" : "iteration \t error\n");
-            int nprint = nh < hcap ? nh : hcap;
-            if (algopt == 1 && status == CSEM_ST_CONVERGED) nprint--; /* the converged value is not logged */
+            const int nprint = csem_history_logged(algopt, preco, status, nh < hcap ? nh : hcap);
             for (int q = 0; q < nprint; q++) fprintf(fp, "%d \t %e\n", q, hist[q]);
             fclose(fp);
           }

@@ -152,9 +152,8 @@ static void run(int algopt, int preco, csem_z *x, csem_z *b, int niter_total, in
   if (csem_solve_fp64_host(g_ctx, algopt, preco, niter_total, tol, m, g_mp, IOM, (const double *)b, (double *)x, h,
                            cap, &nh, &it, &st))
     fail(tag);
-  if (verb) {
-    int nprint = nh < cap ? nh : cap;
-    if (st == CSEM_ST_CONVERGED) nprint--; /* the reference logs a value at the top of the next step */
+  if (verb && st != CSEM_ST_ZERO_RHS) {
+    const int nprint = csem_history_logged(algopt, preco, st, nh < cap ? nh : cap);
     FILE *fp = fopen(fname, "w");
     if (fp) {
       fprintf(fp, algopt == 1 ? "iteration \t relres\n" : "iteration \t error\n");

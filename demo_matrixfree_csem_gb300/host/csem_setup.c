@@ -19,6 +19,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include "../../include/csem_host.h"
+#include "../../include/csem_gpu.h" /* CSEM_ST_* */
 
 #define CSEM_PI 3.14159265358979323846264
 
@@ -572,6 +573,13 @@ void csem_acq_free(csem_acq_t *a)
 }
 
 /* ------------------------------------------------------------------ output */
+int csem_history_logged(int algopt, int preco, int status, int nh)
+{
+  if (nh <= 0 || status == CSEM_ST_ZERO_RHS) return 0;
+  if (algopt == 1) return nh > 1 ? nh - 1 : 1;
+  return preco == 0 && status == CSEM_ST_CONVERGED ? nh - 1 : nh;
+}
+
 int csem_write_emf(const char *fname, int isrc, int nchrec, int nfreq, int nrec, const float *dcal)
 {
   FILE *fp = fopen(fname, "w");

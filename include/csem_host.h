@@ -107,7 +107,17 @@ int csem_acq_check(const csem_acq_t *a, const csem_grid_t *g);
 void csem_acq_free(csem_acq_t *a);
 
 /* ---------------------------------------------------------------- output ---
- * emf_NNNN.txt as write_data (write_data.c:15-37): header line, then
+ * How many entries of a residual history (nh values: the initial one, then one per
+ * BiCGStab step or GMRES inner step) the reference writes to iterate_*.txt:
+ *  - bicgstab / fbicgstab log the previous step's residual at the top of each step
+ *    (solver.c:49-54,136-141), so the last one computed is never logged;
+ *  - gmres (no preconditioner) stops on convergence before logging that residual
+ *    (solver.c:251-255); fgmres logs it first (solver.c:474-481);
+ *  - a zero right-hand side logs nothing: the solvers return before opening the file.
+ * algopt 1 BiCGStab, 2 GMRES; preco 0 none; status a CSEM_ST_* value (csem_gpu.h). */
+int csem_history_logged(int algopt, int preco, int status, int nh);
+
+/* emf_NNNN.txt as write_data (write_data.c:15-37): header line, then
  * "iTx iRx ichrec ifreq re im" in ichrec > ifreq > irec order, values printed %e
  * from complex64. dcal is complex64 interleaved [nchrec][nfreq][nrec][2]. */
 int csem_write_emf(const char *fname, int isrc, int nchrec, int nfreq, int nrec,

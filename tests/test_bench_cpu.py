@@ -1,0 +1,55 @@
+"""Host logic of bench.py on CPU: the roofline arithmetic, the committed traffic figures it
+reads, and the waves the default configuration walks."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_measured_traffic_reads_committed_profiles():
+    import bench
+    lus = bench.measured_traffic("lusgs32")
+    st = bench.measured_traffic("stencil32")
+    assert isinstance(lus, int) and isinstance(st, int)
+    # the captures' DRAM bytes per system are of the order of the algorithmic bytes
+    assert 0.5 < lus / (48 * 11911680) < 3.0
+    assert 0.5 < st / (20 * 11064870) < 3.0
+    assert bench.measured_traffic("A64") is None
+
+
+def test_roofline_arithmetic():
+    import bench
+    res = {"lE": 11064870, "n1": 200, "n2": 140, "n3f": 140,
+           # operator: (summed ms, applications, system-applications)
+           "prof": {"stencil32": (1000.0, 100, 1600), "lusgs32": (7000.0, 100, 1600)}}
+    dom, out = bench.roofline(res, {"hbm_gbs": 6689.5})
+    assert dom == "lusgs32"
+    nf = 200 * 141 * 141 + 201 * 140 * 141 + 201 * 141 * 140
+    r = out["lusgs32"]
+    assert r["algorithmic_bytes_per_system"] == 48 * nf
+    # 16 systems per application, 70 ms per application
+    assert r["achieved"] == pytest.approx(48 * nf * 16 / 0.070 / 1e9, abs=0.1)
+    assert r["frac"] == pytest.approx(r["achieved"] / 6689.5, abs=1e-3)
+    assert r["traffic"] == round(bench.measured_traffic("lusgs32") * 16)
+    assert out["stencil32"]["achieved"] == pytest.approx(20 * 11064870 * 16 / 0.010 / 1e9, abs=0.1)
+    # another grid: no captured traffic applies
+    res["lE"] = 123
+    assert bench.roofline(res, {})[1]["lusgs32"]["traffic"] is None
+
+
+def test_default_waves_cover_the_batch_once():
+    import bench
+    from demo_matrixfree_csem_gb300 import synthetic
+    cfg = synthetic.workload("marlim_like_96")  # the model in memory; nothing written
+    freqs = [float(f) for f in cfg.params["freqs"].split(",")]
+    systems = [(f, s) for f in freqs for s in range(len(cfg.acq.src))]
+    assert len(systems) == 96 and len(freqs) == 6
+    seen = []
+    for k in range(2):  # the default: 2 timed steps of 48
+        f, src = bench.wave_systems(cfg, systems, 48, k, 0)
+        assert len(f) == 48 and src.shape == (48, 3)
+        seen += [(float(a), tuple(b)) for a, b in zip(f, src)]
+    assert len(set(seen)) == 96

@@ -104,3 +104,20 @@ def test_input_errors_are_codes(csem_lib, tmp_path):
     with pytest.raises(cs.CsemError) as e:
         cs.Grid.from_files(*(str(tmp_path / n) for n in ("fx1", "fx2", "fx3", "r1", "r2", "r3")))
     assert e.value.code == -2 and "size not match" in str(e.value)
+
+
+def test_history_logging_rule(csem_lib):
+    """How many residual-history entries the reference writes to iterate_*.txt
+    (csem_history_logged): BiCGStab never logs the last residual it computed; gmres does
+    not log a converged one, fgmres does; a zero right-hand side logs nothing."""
+    import demo_matrixfree_csem_gb300 as cs
+    f = cs.lib().csem_history_logged
+    f.argtypes = [ctypes.c_int] * 4
+    CONV, MAXIT, ZERO = 1, 2, 5
+    assert f(1, 1, CONV, 5) == 4      # converged in the 4th step: initial + 3 logged
+    assert f(1, 0, MAXIT, 9) == 8     # niter=8: initial + steps 1..7
+    assert f(1, 1, MAXIT, 1) == 1     # niter=0: the initial residual only
+    assert f(2, 0, CONV, 12) == 11    # gmres: the converged residual is not logged
+    assert f(2, 3, CONV, 12) == 12    # fgmres: it is
+    assert f(2, 0, MAXIT, 31) == 31
+    assert f(1, 1, ZERO, 0) == 0 and f(2, 3, ZERO, 1) == 0
