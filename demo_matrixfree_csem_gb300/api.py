@@ -110,6 +110,8 @@ def lib(build_if_missing: bool = True):
         "csem_cdot_dev": (C.c_int, [C.c_int, C.c_long, C.c_int, C.c_void_p, C.c_void_p, _dp, C.c_void_p]),
         "csem_solve_batch_host": (C.c_int, [C.c_void_p, C.c_int, _fp, _fp, C.c_int, _ip, C.c_int, _ip, C.c_int, _fp,
                                             C.c_void_p, _dp, _ip, _ip, _ip, _dp]),
+        "csem_csr_compare": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, _dp]),
+        "csem_history_logged": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int]),
         "csem_profile": (C.c_int, [C.c_int]),
         "csem_profile_read": (C.c_int, [C.c_int, _dp, _lp, _lp]),
         "csem_launch_count": (C.c_longlong, []),
@@ -320,6 +322,14 @@ class Ctx:
         _check(lib().csem_extract_host(self.h, len(ch), _p(ch, _ip), len(r), _p(r, _fp),
                                        _p(x.view(np.float64)), _p(out.view(np.float64))))
         return out
+
+    def csr_compare(self, iom: complex, prec: int = 64, nrep: int = 5) -> dict:
+        """The operator assembled in CSR (by probing) against the matrix-free stencil:
+        ms per cuSPARSE SpMV and per stencil application, their max relative difference,
+        stored entries and the bytes one SpMV moves (csem_csr_compare; airbc=0 only)."""
+        out = (C.c_double * 5)()
+        _check(lib().csem_csr_compare(self.h, int(prec), iom.real, iom.imag, int(nrep), out))
+        return dict(ms_csr=out[0], ms_stencil=out[1], relerr=out[2], nnz=int(out[3]), csr_bytes=out[4])
 
     def solve_fp64(self, iom: complex, b, algopt=1, preco=1, niter=1000, tol=1e-8, nrestart=10, mp=30, x0=None):
         """Returns (x, history, iterations, status)."""

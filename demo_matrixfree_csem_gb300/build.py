@@ -27,7 +27,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["k_fdfd.cu", "k_airwave.cu", "k_lusgs.cu", "k_lusgs2.cu", "k_blas.cu", "k_scalar.cu", "k_acq.cu",
-              "engine_model.cu", "solve_fp64.cu", "solve_mixed.cu", "prof.cu", "capi.cu", "capi_noalloc.cu"]
+              "engine_model.cu", "solve_fp64.cu", "solve_mixed.cu", "prof.cu", "capi.cu", "capi_noalloc.cu",
+              "csr_compare.cu"]
 C_SOURCES = ["csem_getpar.c", "csem_setup.c"]
 DRIVER_SOURCES = ["csem_main.c"]
 
@@ -94,7 +95,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if force or _newer(LIB, objs):
         cuda_lib = os.path.join(CUDA_HOME, "lib64")
         tmp = LIB + ".tmp"
-        _run(["g++", "-shared", "-o", tmp, *objs, f"-L{cuda_lib}", "-lcufft", "-lcudart",
+        _run(["g++", "-shared", "-o", tmp, *objs, f"-L{cuda_lib}", "-lcufft", "-lcusparse", "-lcudart",
               f"-Wl,-rpath,{cuda_lib}"], verbose)
         os.replace(tmp, LIB)
     refabi_src = os.path.join(HOST, "csem_refabi.c")

@@ -649,6 +649,19 @@ int csem_aphi_apply_dev(csem_ctx* c, int prec, int nsys, const double* iom, cons
   API_BEGIN return op_dev(c, OP_APHI, prec, nsys, iom, x, y, stream); API_END
 }
 
+int csem_csr_compare(csem_ctx* c, int prec, double iom_re, double iom_im, int nrep, double* out)
+{
+  if (prec != 64 && prec != 32) return csem_set_error(CSEM_EINVAL, "prec must be 64 or 32");
+  if (nrep < 1) return csem_set_error(CSEM_EINVAL, "nrep must be >= 1");
+  if (c->model->airbc)
+    return csem_set_error(CSEM_EINVAL, "the assembled operator has no airwave coupling: airbc=0 only (as Acsr.c)");
+  if ((double)c->model->lE * 13 > 2147483647.0)
+    return csem_set_error(CSEM_ETOOBIG, "more than 2^31 stored entries: 32-bit CSR indices do not reach");
+  API_BEGIN
+  csr_compare(c->model, c->st, prec, iom_re, iom_im, nrep, out);
+  API_END
+}
+
 int csem_cdot_dev(int prec, long n, int nsys, const void* a, const void* b, double* out_dev, void* stream)
 {
   if (prec != 64 && prec != 32) return csem_set_error(CSEM_EINVAL, "prec must be 64 or 32");

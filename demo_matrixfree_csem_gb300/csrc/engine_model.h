@@ -105,4 +105,9 @@ class Ops {
 SysScal<F64> sys_scal64(double iom_re, double iom_im);
 SysScal<F32> sys_scal32(const SysScal<F64>& s);
 
+// The operator assembled in CSR by probing the stencil, timed against it with cuSPARSE's
+// SpMV (csr_compare.cu); out: ms per SpMV, ms per stencil, max relative difference, nnz,
+// bytes one SpMV moves. Model without airwave coupling only.
+void csr_compare(Model* m, cudaStream_t st, int prec, double iom_re, double iom_im, int nrep, double* out);
+
 }  // namespace csem

@@ -3,6 +3,10 @@
     python -m demo_matrixfree_csem_gb300.opbench --workload marlim_like_96 --op lusgs \
         --prec 32 --nsys 16 --reps 5 [--schedule pipelined|diagonal] [--vw 0|1|2|4]
 
+--op csr compares the matrix-free operator with the same operator assembled in CSR and
+applied by cuSPARSE (csem_csr_compare), on the workload's grid without the airwave (the
+assembled operator has no airwave coupling), one system.
+
 Vectors are random and stay on the device; each repetition applies the operator to all
 systems once through the device-pointer C ABI (csem_*_apply_dev) on the context's
 stream, timed with CUDA events on that stream. Prints one JSON line: milliseconds per
@@ -24,7 +28,7 @@ import numpy as np
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--workload", default="marlim_like_96")
-    ap.add_argument("--op", choices=["A", "lusgs", "aphi"], default="lusgs")
+    ap.add_argument("--op", choices=["A", "lusgs", "aphi", "csr"], default="lusgs")
     ap.add_argument("--prec", type=int, choices=[32, 64], default=32)
     ap.add_argument("--nsys", type=int, default=16)
     ap.add_argument("--reps", type=int, default=5)
@@ -37,10 +41,22 @@ def main(argv=None) -> None:
     import torch
     from . import api, synthetic
     cfg = synthetic.workload(a.workload)
+    if a.op == "csr":
+        cfg.params["airbc"] = 0
     airbc = int(cfg.params.get("airbc", 0))
     with tempfile.TemporaryDirectory() as d:
         G = synthetic.build_grid(cfg, d)
     ctx = api.Ctx(G, airbc, 0)
+    if a.op == "csr":
+        r = ctx.csr_compare(api.iom_of(a.freq), a.prec, a.reps)
+        st_bytes = (2 * (16 if a.prec == 64 else 8) + (8 if a.prec == 64 else 4)) * ctx.lE
+        r.update(workload=a.workload, airbc=0, prec=a.prec, unknowns=ctx.lE,
+                 csr_GBps=r["csr_bytes"] / (r["ms_csr"] * 1e-3) / 1e9,
+                 stencil_algorithmic_bytes=st_bytes,
+                 stencil_GBps=st_bytes / (r["ms_stencil"] * 1e-3) / 1e9,
+                 csr_over_stencil_time=r["ms_csr"] / r["ms_stencil"])
+        print(json.dumps(r), flush=True)
+        return
     ctx.set_option("lusgs_pipelined", 1 if a.schedule == "pipelined" else 0)
     ctx.set_option("lusgs_vw", a.vw)
     dt = torch.complex64 if a.prec == 32 else torch.complex128

@@ -187,6 +187,15 @@ int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, doub
  *  - nothing needs clearing beforehand: each call writes every partial it reads. */
 #define CSEM_NOALLOC_DOT_MAX_SYSTEMS 64
 int csem_cdot_dev_noalloc(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
+/* The assembled operator as a comparison point (Acsr_init / Acsr_apply, Acsr.c:704-716,
+ * which the reference uses only as a check): A is assembled in CSR on the device by
+ * probing the matrix-free operator with 81 indicator vectors (13 stored entries per
+ * row, 32-bit indices), then cuSPARSE's SpMV and the stencil are each timed nrep times on
+ * one random vector. out[0] ms per SpMV, out[1] ms per stencil application, out[2] max
+ * relative difference of the two products, out[3] stored entries, out[4] bytes one SpMV
+ * must move (values, indices, row pointers, x, y). prec 64 or 32. airbc=0 only, as the
+ * reference's assembly: the airwave couples the top plane through an FFT. */
+int csem_csr_compare(csem_ctx *c, int prec, double iom_re, double iom_im, int nrep, double *out);
 /* synchronise the context's stream */
 int csem_ctx_sync(csem_ctx *c);
 /* the context's CUDA stream (a cudaStream_t), for callers that record events on it */
