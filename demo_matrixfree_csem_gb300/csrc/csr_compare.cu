@@ -168,10 +168,27 @@ void compare(Model* m, cudaStream_t st, double iom_re, double iom_im, int nrep, 
   CSEM_CUDA_TRY(cudaGetLastError());
   count_launch(), k_random<C><<<nb, 256, 0, st>>>(n, x.as<C>());
 
-  cusparseHandle_t h;
+  // cuSPARSE objects and events, released on every exit (errors throw)
+  struct Res {
+    cusparseHandle_t h = nullptr;
+    cusparseSpMatDescr_t A = nullptr;
+    cusparseDnVecDescr_t X = nullptr, Y = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Res()
+    {
+      if (X) cusparseDestroyDnVec(X);
+      if (Y) cusparseDestroyDnVec(Y);
+      if (A) cusparseDestroySpMat(A);
+      if (h) cusparseDestroy(h);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } res;
+  cusparseHandle_t& h = res.h;
+  cusparseSpMatDescr_t& A = res.A;
+  cusparseDnVecDescr_t &X = res.X, &Y = res.Y;
+  cudaEvent_t &e0 = res.e0, &e1 = res.e1;
   CSEM_SPARSE_TRY(cusparseCreate(&h));
-  cusparseSpMatDescr_t A;
-  cusparseDnVecDescr_t X, Y;
   const cudaDataType dt = P::exact ? CUDA_C_64F : CUDA_C_32F;
   CSEM_SPARSE_TRY(cusparseSetStream(h, st));
   CSEM_SPARSE_TRY(cusparseCreateCsr(&A, n, n, n * SLOTS, rp.p, col.p, val.p, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_32I,
@@ -187,7 +204,6 @@ void compare(Model* m, cudaStream_t st, double iom_re, double iom_im, int nrep, 
   CSEM_SPARSE_TRY(cusparseSpMV_bufferSize(h, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, A, X, &zero, Y, dt,
                                           CUSPARSE_SPMV_ALG_DEFAULT, &wb));
   work.alloc(wb > 0 ? wb : 16);
-  cudaEvent_t e0, e1;
   CSEM_CUDA_TRY(cudaEventCreate(&e0));
   CSEM_CUDA_TRY(cudaEventCreate(&e1));
   auto spmv = [&]() {
@@ -219,12 +235,6 @@ void compare(Model* m, cudaStream_t st, double iom_re, double iom_im, int nrep, 
     if (d > dmax) dmax = d;
     if (yy > ymax) ymax = yy;
   }
-  cusparseDestroyDnVec(X);
-  cusparseDestroyDnVec(Y);
-  cusparseDestroySpMat(A);
-  cusparseDestroy(h);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   out[0] = ms_csr / nrep;
   out[1] = ms_st / nrep;
   out[2] = ymax > 0 ? std::sqrt(dmax / ymax) : 0.0;
