@@ -1,11 +1,12 @@
-"""Receiver fixtures of the 120^3 workloads computed by the reference itself.
+"""Receiver fixtures of whole workloads computed by the reference itself.
 
 The reference (built from its sources by oracle/build_ref.sh) solves a workload of
 demo_matrixfree_csem_gb300.synthetic - layered_120 (100^3 core cells of 100 m, nb=10
-padding to 120^3, airbc=1, one Ex dipole at (0,0,950), 101 seafloor receivers) or
+padding to 120^3, airbc=1, one Ex dipole at (0,0,950), 101 seafloor receivers),
 vti_block_120 (the same grid, rho33 = 2 rho11, a 50 ohm-m 2 x 2 x 0.1 km block at
-2050 m) - with BiCGStab + LU-SGS to tol=1e-8/f, one frequency per process, and this
-script stores for each frequency:
+2050 m) or bathymetry_125 (125 x 125 x 100 cells of 100 m under a seafloor of three
+Gaussian hills, nb=10, its first source) - with BiCGStab + LU-SGS to tol=1e-8/f, one
+frequency per process, and this script stores for each frequency:
   * the receivers in complex128 (the value extract_emf computes before its complex64
     store; the oracle's extraction is bit-identical to it), channels Ex, Ey, Ez;
   * the complex64 values the reference stores in dcal_fd;
@@ -21,7 +22,7 @@ Makefile's -O3 gives with GCC on aarch64, oracle/build_ref.sh) and the output is
 reference_receivers_fma.npz: the same solves from a second, equally valid build of the
 reference, which measures how far the reference's receivers move with rounding alone.
 
-    python tests/golden/make_reference_receivers.py [layered_120|vti_block_120]
+    python tests/golden/make_reference_receivers.py [layered_120|vti_block_120|bathymetry_125]
     CSEM_REF_VARIANT=fma python tests/golden/make_reference_receivers.py vti_block_120
 """
 from __future__ import annotations
@@ -50,7 +51,7 @@ def one(workload: str, ifreq: int, work: str) -> None:
     cfg = synthetic.workload(workload)
     synthetic.write_config(cfg, work)
     os.chdir(work)
-    R = Ref(cfg.args(work))
+    R = Ref(cfg.args(work) + ["preco=1", "algopt=1"])  # BiCGStab + LU-SGS, whatever the workload's default
     x, b, t = R.solve(ifreq, verb=1)
     hist = []
     with open("iterate_fbicgstab.txt") as f:

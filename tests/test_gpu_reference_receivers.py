@@ -1,7 +1,7 @@
-"""Whole solves of the 120^3 workloads against the reference's own receivers.
+"""Whole solves of full workloads against the reference's own receivers.
 
-The fixtures tests/golden/<workload>/reference_receivers.npz (layered_120, and
-vti_block_120 when present) were computed by the reference itself (built from its
+The fixtures tests/golden/<workload>/reference_receivers.npz (layered_120, vti_block_120
+and bathymetry_125, each where present) were computed by the reference itself (built from its
 sources, FFTW replaced by the oracle's DFT; tests/golden/make_reference_receivers.py)
 with BiCGStab + LU-SGS to tol = 1e-8/f at 0.25, 0.75 and 1.25 Hz. Errors are max-norm
 relative per frequency and channel. Ey is zero by symmetry on the receiver line (its
@@ -35,8 +35,9 @@ from demo_matrixfree_csem_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-WORKLOADS = [w for w in ("layered_120", "vti_block_120")
-             if os.path.exists(os.path.join(GOLDEN, w, "reference_receivers.npz"))]
+WORKLOADS = [w for w in ("layered_120", "vti_block_120", "bathymetry_125")
+             if all(os.path.exists(os.path.join(GOLDEN, w, f))
+                    for f in ("reference_receivers.npz", "reference_receivers_fma.npz"))]
 
 
 @pytest.fixture(scope="module", params=WORKLOADS)
