@@ -69,6 +69,8 @@ def test_fp64_dropin_matches_reference(gpu, layered):
         x, hist, it, st = ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=1000, tol=tol)
         assert st == "converged"
         err = _errors(ctx.extract_emf(["Ex", "Ey", "Ez"], cfg.acq.rec, x), z["rec"][f])
+        print(f"{freq} Hz: errors {err}, reference spread {z['spread'][f]:.2e}, iterations {it} "
+              f"(reference {len(z[f'hist{f}']) - 1})")
         assert max(err) <= max(1e-9, 5 * z["spread"][f]), (freq, err, z["spread"][f])
         href = z[f"hist{f}"]
         assert abs(it - (len(href) - 1)) <= 0.2 * (len(href) - 1), (freq, it, len(href) - 1)
