@@ -22,7 +22,7 @@ Makefile's -O3 gives with GCC on aarch64, oracle/build_ref.sh) and the output is
 reference_receivers_fma.npz: the same solves from a second, equally valid build of the
 reference, which measures how far the reference's receivers move with rounding alone.
 
-    python tests/golden/make_reference_receivers.py [layered_120|vti_block_120|bathymetry_125]
+    python tests/golden/make_reference_receivers.py [layered_120|vti_block_120|bathymetry_125|marlim_like_96]
     CSEM_REF_VARIANT=fma python tests/golden/make_reference_receivers.py vti_block_120
 """
 from __future__ import annotations
@@ -76,19 +76,21 @@ def main() -> None:
         sys.exit("reference sources not found")
     build_ref()
     os.makedirs(os.path.join(HERE, workload), exist_ok=True)
+    from demo_matrixfree_csem_gb300 import synthetic
+    nf = len(synthetic.workload(workload).params["freqs"].split(","))  # one process per frequency
     tmp = tempfile.mkdtemp(prefix="_work_", dir=os.path.join(HERE, workload))  # removed at the end
-    works = [os.path.join(tmp, f"w{i}") for i in range(3)]
+    works = [os.path.join(tmp, f"w{i}") for i in range(nf)]
     for w in works:
         os.makedirs(w)
-    with cf.ThreadPoolExecutor(3) as ex:
+    with cf.ThreadPoolExecutor(nf) as ex:
         list(ex.map(lambda i: subprocess.run([sys.executable, __file__, workload, str(i), works[i]], check=True,
-                                             stdout=subprocess.DEVNULL), range(3)))
-    parts = [np.load(os.path.join(works[i], f"f{i}.npz")) for i in range(3)]
+                                             stdout=subprocess.DEVNULL), range(nf)))
+    parts = [np.load(os.path.join(works[i], f"f{i}.npz")) for i in range(nf)]
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     np.savez_compressed(OUT, rec=np.stack([p["rec"] for p in parts]), dcal=np.stack([p["dcal"] for p in parts]),
                         freqs=np.array([float(p["freq"]) for p in parts], np.float32),
-                        hist0=parts[0]["hist"], hist1=parts[1]["hist"], hist2=parts[2]["hist"],
-                        seconds=np.array([float(p["seconds"]) for p in parts]))
+                        seconds=np.array([float(p["seconds"]) for p in parts]),
+                        **{f"hist{i}": parts[i]["hist"] for i in range(nf)})
     shutil.rmtree(tmp)
     print("wrote", OUT)
 
