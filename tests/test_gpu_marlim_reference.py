@@ -47,3 +47,26 @@ def test_mixed_batch_matches_reference_on_bench_workload(gpu):
                for c in range(3)]
         print(f"{float(freqs[q])} Hz: mixed vs reference {err}")
         assert max(err) <= 1e-7, (float(freqs[q]), err)
+
+
+@pytest.mark.skipif(not os.path.exists(FIXTURE), reason="no reference receivers of the bench workload")
+def test_fp64_dropin_matches_reference_on_bench_workload(gpu):
+    """The plain complex128 drop-in at the highest frequency: within 1e-9 of the reference."""
+    z = np.load(FIXTURE)
+    cfg = synthetic.workload("marlim_like_96")
+    f = len(z["freqs"]) - 1
+    with tempfile.TemporaryDirectory() as d:
+        G = synthetic.build_grid(cfg, d)
+    ctx = cs.Ctx(G, 1, 0)
+    freq = float(z["freqs"][f])
+    iom = cs.iom_of(freq)
+    b = ctx.inject_source(iom, ["Ex"], cfg.acq.src[0])
+    tol = float(np.float32(np.float32(1e-8) / np.float32(freq)))
+    x, hist, it, st = ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=1000, tol=tol)
+    assert st == "converged"
+    ref = z["rec"][f]
+    out = ctx.extract_emf(["Ex", "Ey", "Ez"], cfg.acq.rec, x)
+    ex = np.abs(ref[0]).max()
+    err = [float(np.abs(out[c] - ref[c]).max() / (np.abs(ref[c]).max() if c != 1 else ex)) for c in range(3)]
+    print(f"{freq} Hz: complex128 vs reference {err}, iterations {it} (reference {len(z[f'hist{f}']) - 1})")
+    assert max(err) <= 1e-9, (freq, err)
