@@ -516,7 +516,14 @@ int csem_solve_batch_host(csem_ctx* c, int nsys, const float* freq, const float*
     return csem_set_error(CSEM_EINVAL, "algopt must be 1 (BiCGStab) or 2 (GMRES)");
   if (opt->precision == 32 && opt->algopt == 2 && (opt->nrestart < 1 || opt->nrestart > 64))
     return csem_set_error(CSEM_EINVAL, "nrestart must be in 1..64");
+  if (opt->precision == 64) {  // the reference's dispatch (main.c:104-118) on one system at a time
+    if (opt->algopt != 1 && opt->algopt != 2) return csem_set_error(CSEM_EINVAL, "algopt must be 1 (BiCGStab) or 2 (GMRES)");
+    if (opt->preco < 0 || opt->preco > 3) return csem_set_error(CSEM_EINVAL, "preco must be 0..3");
+    if (opt->algopt == 2 && opt->nrestart < 1) return csem_set_error(CSEM_EINVAL, "nrestart must be >= 1");
+    if (opt->preco == 2 && opt->mp < 1) return csem_set_error(CSEM_EINVAL, "mp must be >= 1");
+  }
   if (nchsrc < 1 || nchsrc > 8) return csem_set_error(CSEM_EINVAL, "1..8 source channels");
+  if (!c) return csem_set_error(CSEM_EINVAL, "csem_solve_batch_host: no context");
   API_BEGIN
   std::vector<double> iom(2 * nsys), tol(nsys);
   for (int s = 0; s < nsys; s++) {
@@ -662,18 +669,27 @@ int csem_csr_compare(csem_ctx* c, int prec, double iom_re, double iom_im, int nr
   API_END
 }
 
+static constexpr int kMaxDotDevices = 64;
+
 int csem_cdot_dev(int prec, long n, int nsys, const void* a, const void* b, double* out_dev, void* stream)
 {
   if (prec != 64 && prec != 32) return csem_set_error(CSEM_EINVAL, "prec must be 64 or 32");
+  if (n < 1 || nsys < 1) return csem_set_error(CSEM_EINVAL, "csem_cdot_dev: n and nsys must be positive");
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return csem_set_error(CSEM_ENODEV, "no CUDA device available");
+  if (dev >= kMaxDotDevices) return csem_set_error(CSEM_EINVAL, "csem_cdot_dev: device %d beyond the %d supported", dev,
+                                                   kMaxDotDevices);
   API_BEGIN
   const int nblk = dot_blocks(n);
-  static thread_local DevBuf part;  // callers on different threads use different streams
-  ensure(part, sizeof(double2) * (size_t)nblk * nsys);
+  // one partial-sum buffer per host thread and device: a buffer is only ever handed to
+  // kernels on the device it was allocated on
+  static thread_local DevBuf part[kMaxDotDevices];
+  ensure(part[dev], sizeof(double2) * (size_t)nblk * nsys);
   if (prec == 64)
-    launch_dot<F64>((const double2*)a, (const double2*)b, n, n, nsys, nullptr, part.as<double2>(), nblk,
+    launch_dot<F64>((const double2*)a, (const double2*)b, n, n, nsys, nullptr, part[dev].as<double2>(), nblk,
                     (double2*)out_dev, (cudaStream_t)stream);
   else
-    launch_dot<F32>((const float2*)a, (const float2*)b, n, n, nsys, nullptr, part.as<double2>(), nblk,
+    launch_dot<F32>((const float2*)a, (const float2*)b, n, n, nsys, nullptr, part[dev].as<double2>(), nblk,
                     (double2*)out_dev, (cudaStream_t)stream);
   CSEM_CUDA_TRY(cudaGetLastError());
   API_END

@@ -13,7 +13,8 @@
 //    systems x the at most 1024 blocks one dot product is split into);
 //  - the array's device address is looked up with cudaGetSymbolAddress once per device,
 //    on the first call made with that device current, and cached; make that first call
-//    before any stream capture starts;
+//    before any stream capture starts. The cache is never refreshed, so a
+//    cudaDeviceReset of that device between two calls is not supported;
 //  - the array is one per device for the whole process: calls on the same device that
 //    overlap in time (other streams, other host threads) race on it and return wrong
 //    results, so serialise them, e.g. on one stream;

@@ -170,7 +170,11 @@ int csem_batch_capacity(csem_ctx *c, int precision, int preco, double budget_byt
 int csem_fdfd_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
 int csem_lusgs_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
 int csem_aphi_apply_dev(csem_ctx *c, int prec, int nsys, const double *iom, const void *x, void *y, void *stream);
-/* out[s] (complex128, device) = <a_s, b_s> for nsys vectors of length n (stride n) */
+/* out[s] (complex128, device) = <a_s, b_s> for nsys vectors of length n (stride n).
+ * The per-block partial sums live in a buffer the library allocates on first use, one
+ * per host thread and device, and grows on demand. Calls from one host thread on one
+ * device share that buffer: two such calls on different streams that overlap in time
+ * race on it, so order them (one stream, or an event between them). */
 int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
 /* The same dot products, identical bits, without any device allocation by the library.
  * No counterpart in the reference (its cdotprod, cdotprod.c:13-19, is a host loop).
@@ -184,7 +188,9 @@ int csem_cdot_dev(int prec, long n, int nsys, const void *a, const void *b, doub
  *    cudaGetSymbolAddress and caches it: make that call before any stream capture starts;
  *  - the array is shared by all calls on a device: calls that overlap in time (other
  *    streams, other host threads) race on it; serialise them;
- *  - nothing needs clearing beforehand: each call writes every partial it reads. */
+ *  - nothing needs clearing beforehand: each call writes every partial it reads;
+ *  - the cached address is not refreshed: calling cudaDeviceReset on a device between
+ *    two calls is not supported (the module, and with it the array, is reloaded). */
 #define CSEM_NOALLOC_DOT_MAX_SYSTEMS 64
 int csem_cdot_dev_noalloc(int prec, long n, int nsys, const void *a, const void *b, double *out_dev, void *stream);
 /* The assembled operator as a comparison point (Acsr_init / Acsr_apply, Acsr.c:704-716,

@@ -3,7 +3,10 @@
 # oracle/_ref/ (git-ignored). Test infrastructure only: the result is the CPU oracle
 # that pins oracle/csem_oracle.c and generates tests/golden fixtures.
 #
-#   REF=/root/reference oracle/build_ref.sh
+#   REF=<reference checkout> oracle/build_ref.sh
+#
+# REF defaults to CSEM_REFERENCE_DIR, else to a sibling directory "reference" of this
+# repository.
 #
 # Sources: every reference .c except Acoo.c (MUMPS direct solver, reached only from the
 # dead main3 in main.c:226-280; MUMPS is not installed). MPI and FFTW are replaced by
@@ -16,7 +19,7 @@
 # aarch64, used to measure how far the reference's own results move between builds.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${REF:-/root/reference}"
+REF="${REF:-${CSEM_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}}"
 CONTRACT="-ffp-contract=off"
 OUT="$HERE/_ref"
 if [ "${REF_VARIANT:-}" = "fma" ]; then

@@ -15,7 +15,9 @@ ORACLE_LIB = os.path.join(HERE, "_build", "libcsemoracle.so")
 # CSEM_REF_VARIANT=fma selects the multiply-add-contracting build (build_ref.sh)
 REF_VARIANT = os.environ.get("CSEM_REF_VARIANT", "")
 REF_LIB = os.path.join(HERE, "_ref_fma" if REF_VARIANT == "fma" else "_ref", "libcsemref.so")
-REF_SRC = os.environ.get("CSEM_REFERENCE_DIR", "/root/reference")
+# the reference checkout: CSEM_REFERENCE_DIR, else a sibling directory "reference" of this
+# repository
+REF_SRC = os.environ.get("CSEM_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

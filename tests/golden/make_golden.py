@@ -11,7 +11,8 @@ functions on tiny seeded models. For each case this writes:
       x after `niter` solver iterations, the relative-residual history of that run
       (the value the reference prints), and the receivers it extracts (complex64).
 
-Run in a checkout where the reference sources exist (default /root/reference):
+Run where the reference sources exist (CSEM_REFERENCE_DIR, else a sibling directory
+"reference" of this repository):
     python tests/golden/make_golden.py
 The fixtures are committed; the tests only read them.
 """

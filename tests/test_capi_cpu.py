@@ -121,3 +121,42 @@ def test_history_logging_rule(csem_lib):
     assert f(2, 3, CONV, 12) == 12    # fgmres: it is
     assert f(2, 0, MAXIT, 31) == 31
     assert f(1, 1, ZERO, 0) == 0 and f(2, 3, ZERO, 1) == 0
+
+
+def test_batch_options_are_checked_before_any_device_work(csem_lib):
+    """csem_solve_batch_host rejects option combinations the solvers cannot run with
+    CSEM_EINVAL before it touches the context or the GPU: GMRES without a restart length
+    (the reference runs niter / nrestart cycles, main.c:106,109), the inner-GMRES
+    preconditioner without steps, preconditioners and algorithms out of range, for both
+    precisions."""
+    import demo_matrixfree_csem_gb300 as cs
+    from demo_matrixfree_csem_gb300.api import _BatchOpts
+    L = cs.lib()
+    f = np.array([1.0], np.float32)
+    s = np.zeros(3, np.float32)
+    ch = np.zeros(1, np.int32)
+    out = np.zeros(2)
+    it = np.zeros(1, np.int32)
+
+    def call(**kw):
+        d = dict(precision=64, algopt=1, preco=1, niter=10, tol=1e-8, inner_tol=0.2, check_every=4, max_outer=30,
+                 nrestart=10, mp=30)
+        d.update(kw)
+        o = _BatchOpts(*[d[k] for k in ("precision", "algopt", "preco", "niter", "tol", "inner_tol", "check_every",
+                                        "max_outer", "nrestart", "mp")])
+        fp = ctypes.POINTER(ctypes.c_float)
+        ip = ctypes.POINTER(ctypes.c_int)
+        dp = ctypes.POINTER(ctypes.c_double)
+        return L.csem_solve_batch_host(None, 1, f.ctypes.data_as(fp), s.ctypes.data_as(fp), 1, ch.ctypes.data_as(ip),
+                                       1, ch.ctypes.data_as(ip), 0, s.ctypes.data_as(fp), ctypes.byref(o),
+                                       out.ctypes.data_as(dp), it.ctypes.data_as(ip), it.ctypes.data_as(ip),
+                                       it.ctypes.data_as(ip), out.ctypes.data_as(dp))
+
+    EINVAL = -1
+    assert call(precision=64, algopt=2, nrestart=0) == EINVAL
+    assert call(precision=64, preco=2, mp=0) == EINVAL
+    assert call(precision=64, preco=4) == EINVAL
+    assert call(precision=64, algopt=3) == EINVAL
+    assert call(precision=32, algopt=2, nrestart=0) == EINVAL
+    assert call(precision=32, preco=2) == EINVAL
+    assert call(precision=16) == EINVAL

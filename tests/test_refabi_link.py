@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("CSEM_REFERENCE_DIR", "/root/reference")
+from oracle.pyoracle import REF_SRC as REF  # noqa: E402
 pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(REF, "main.c")),
                                 reason="reference sources not present")
 
