@@ -29,6 +29,8 @@ struct csem_ctx {
   int nmax64 = 0, nmax32 = 0;
   bool lusgs_pipelined = true;
   int lusgs_vw = 0;
+  bool lusgs_tiled = false;
+  int tile_rows = 8, tile_vw = 4;
   bool autotune = false;
   bool graphs = true;
   bool seq_dots = false;
@@ -39,6 +41,9 @@ template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
 {
   o.pipelined_sweeps = c->lusgs_pipelined;
   o.sweep_vw = c->lusgs_vw;
+  o.tiled_sweeps = c->lusgs_tiled;
+  o.tile_rows = c->tile_rows;
+  o.tile_vw = c->tile_vw;
 }
 
 #define API_BEGIN try {
@@ -160,6 +165,14 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     if (value != 0 && value != 1 && value != 2 && value != 4)
       return csem_set_error(CSEM_EINVAL, "lusgs_vw must be 0, 1, 2 or 4");
     c->lusgs_vw = value;
+  } else if (!strcmp(name, "lusgs_tiled")) {
+    c->lusgs_tiled = value != 0;
+  } else if (!strcmp(name, "lusgs_tile_rows")) {
+    if (value != 4 && value != 8 && value != 16) return csem_set_error(CSEM_EINVAL, "lusgs_tile_rows must be 4, 8 or 16");
+    c->tile_rows = value;
+  } else if (!strcmp(name, "lusgs_tile_vw")) {
+    if (value != 1 && value != 2 && value != 4) return csem_set_error(CSEM_EINVAL, "lusgs_tile_vw must be 1, 2 or 4");
+    c->tile_vw = value;
   } else if (!strcmp(name, "autotune")) {
     c->autotune = value != 0;
   } else if (!strcmp(name, "graphs")) {

@@ -63,6 +63,11 @@ template <class P> struct SweepP {
 template <class P>
 void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw);
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK);  // the sweep's rows fit one CTA
+// complex64 line-tiled sweeps (k_lusgs3.cu): 32 lines per CTA, rows in warp blocks of at
+// most rows_per_warp (4, 8, 16), vw march positions per step for Ey/Ez (1, 2, 4)
+void launch_sweep_tiled(const SweepP<F32>& s, int comp, bool fwd, int nslot, cudaStream_t st, int rows_per_warp,
+                        int vw);
+bool sweep_tiled_fits(int comp, int n1, int n2, int nK, int rows_per_warp);  // at most 32 warps
 template <class P>
 void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int nslot, cudaStream_t st);
 int sweep_diagonals(int comp, int n1, int n2, int nK);  // number of diagonals t (2..)

@@ -347,6 +347,12 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
   // both schedules visit the points of a sweep in an order that respects every
   // dependency of the lexicographic sweep, so they may be mixed sweep by sweep
   auto sweep = [&](int comp, bool fwd) {
+    if constexpr (!P::exact) {
+      if (tiled_sweeps && sweep_tiled_fits(comp, n1, n2, s.nK, tile_rows)) {
+        launch_sweep_tiled(s, comp, fwd, nslot, st, tile_rows, tile_vw);
+        return;
+      }
+    }
     if (pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
       launch_sweep_pipelined<P>(s, comp, fwd, nslot, st, sweep_vw);
       return;

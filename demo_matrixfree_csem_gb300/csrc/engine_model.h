@@ -88,6 +88,11 @@ class Ops {
   // false = one launch per wavefront diagonal (k_lusgs.cu); both give identical results
   bool pipelined_sweeps = true;
   int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
+  // complex64 only: line-tiled sweeps (k_lusgs3.cu) instead of the pipelined ones, with
+  // at most tile_rows rows per warp and tile_vw march positions per step (Ey, Ez)
+  bool tiled_sweeps = false;
+  int tile_rows = 8;
+  int tile_vw = 4;
   // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal)
   void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
   // bounds_zero: the caller guarantees that Y's entries outside the swept interior are

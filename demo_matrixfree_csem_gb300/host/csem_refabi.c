@@ -74,6 +74,13 @@ void fdfd_init(emf_t *emf)
   emf->lH = emf->lHx + emf->lHy + emf->lHz;
   emf->lv = (n1 + 1) * (n2 + 1) * (n3 + 1);
   if (csem_ctx_create(g, emf->airbc, emf->fvm, &g_ctx)) fail("fdfd_init");
+  /* dot products in the reference's sequential order on request (flag dot_order=1 of a
+   * driver that links the reference's getpar, or CSEM_DOT_ORDER=1 in the environment) */
+  int dot_order = 0;
+  const char *env = getenv("CSEM_DOT_ORDER");
+  if (env) dot_order = atoi(env);
+  if (getparint) getparint("dot_order", &dot_order);
+  if (dot_order && csem_ctx_set_option(g_ctx, "dot_order", dot_order)) fail("dot_order");
 }
 
 void fdfd_free(emf_t *emf)

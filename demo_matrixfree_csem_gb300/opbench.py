@@ -36,6 +36,11 @@ def main(argv=None) -> None:
     ap.add_argument("--freq", type=float, default=0.5)
     ap.add_argument("--schedule", choices=["pipelined", "diagonal"], default="pipelined")
     ap.add_argument("--vw", type=int, default=0)
+    ap.add_argument("--tiled", type=int, default=0, help="1: line-tiled complex64 LU-SGS sweeps")
+    ap.add_argument("--tile-rows", type=int, default=8)
+    ap.add_argument("--tile-vw", type=int, default=4)
+    ap.add_argument("--check", action="store_true",
+                    help="also apply the operator with the default schedule and report the difference")
     a = ap.parse_args(argv)
 
     import torch
@@ -59,6 +64,9 @@ def main(argv=None) -> None:
         return
     ctx.set_option("lusgs_pipelined", 1 if a.schedule == "pipelined" else 0)
     ctx.set_option("lusgs_vw", a.vw)
+    ctx.set_option("lusgs_tiled", a.tiled)
+    ctx.set_option("lusgs_tile_rows", a.tile_rows)
+    ctx.set_option("lusgs_tile_vw", a.tile_vw)
     dt = torch.complex64 if a.prec == 32 else torch.complex128
     gen = torch.Generator(device="cuda").manual_seed(7)
     x = torch.randn(a.nsys, ctx.lE, dtype=dt, device="cuda", generator=gen)
@@ -91,8 +99,20 @@ def main(argv=None) -> None:
     bc = 16 if a.prec == 64 else 8
     bs = bc // 2
     per_sys = {"A": (2 * bc + bs) * ctx.lE, "lusgs": (5 * bc + 2 * bs) * nf, "aphi": None}[a.op]
+    check = None
+    if a.check:
+        y1 = y.clone()
+        ctx.set_option("lusgs_tiled", 0)
+        ctx.set_option("lusgs_pipelined", 1)
+        ctx.set_option("lusgs_vw", 0)
+        apply()
+        torch.cuda.synchronize()
+        d = (y1 - y).abs().max().item()
+        check = {"max_abs_diff": d, "rel": d / max(y.abs().max().item(), 1e-300),
+                 "bit_identical": bool(torch.equal(torch.view_as_real(y1), torch.view_as_real(y)))}
     out = {"workload": a.workload, "op": a.op, "prec": a.prec, "nsys": a.nsys, "schedule": a.schedule,
-           "vw": a.vw, "ms_per_application": ms, "ms_per_system": ms / a.nsys,
+           "vw": a.vw, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
+           "ms_per_application": ms, "ms_per_system": ms / a.nsys,
            "algorithmic_bytes_per_system": per_sys,
            "algorithmic_GBps": per_sys * a.nsys / (ms * 1e-3) / 1e9 if per_sys else None}
     print(json.dumps(out), flush=True)

@@ -212,6 +212,13 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     lockstep pipeline; 0: one launch per wavefront diagonal;
  *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
  *                     0 for the default (2 complex64, 1 complex128).
+ *   "lusgs_tiled"     complex64 only. 1: line-tiled sweeps - 32 independent lines per CTA
+ *                     (one lane each), the rows cut into one block per warp; 0: the
+ *                     schedule chosen by lusgs_pipelined. Same values as the pipelined
+ *                     complex64 sweeps;
+ *   "lusgs_tile_rows" rows per warp block of the tiled sweeps: 4, 8 (default) or 16;
+ *   "lusgs_tile_vw"   march positions per step of the tiled Ey and Ez sweeps: 1, 2 or 4
+ *                     (default);
  *   "autotune"        1: the batched mixed-precision solve times the complex64 LU-SGS
  *                     sweep variants (points per thread 1, 2, 4) on its first running
  *                     systems and keeps the fastest for that batch; 0 (default): the

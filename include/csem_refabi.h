@@ -21,6 +21,11 @@
  *    the whole solve on the GPU with x and b copied once each way; the history files
  *    (iterate_*.txt) and progress lines keep the reference's format. Other operator
  *    pointers are refused (message and exit(1), as err()).
+ *  - the solvers' dot products use the library's fixed parallel tree; with the flag
+ *    dot_order=1 (read through the reference's getparint when the driver links cstd.c)
+ *    or CSEM_DOT_ORDER=1 in the environment they use the reference's sequential order
+ *    (cdotprod.c:13-19), and a solve without airwave repeats the reference's iterates
+ *    bit for bit;
  *  - errors print "csem_refabi: <message>" and exit(1), as the reference's err() does.
  */
 #ifndef CSEM_REFABI_H
