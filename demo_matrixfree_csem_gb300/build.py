@@ -20,6 +20,8 @@ OUT = os.environ.get("CSEM_BUILD_DIR") or os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libcsem_gpu.so")
 DRIVER = os.path.join(OUT, "csem")
 REFABI = os.path.join(OUT, "libcsem_refabi.so")
+# the host set-up alone (model read, padding, airwave tables; no CUDA), for CPU-only users
+HOST_LIB = os.path.join(OUT, "libcsem_host.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -98,6 +100,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         _run(["g++", "-shared", "-o", tmp, *objs, f"-L{cuda_lib}", "-lcufft", "-lcusparse", "-lcudart",
               f"-Wl,-rpath,{cuda_lib}"], verbose)
         os.replace(tmp, LIB)
+    host_objs = [os.path.join(OUT, s + ".o") for s in C_SOURCES]
+    if force or _newer(HOST_LIB, host_objs):
+        _run(["gcc", "-shared", "-o", HOST_LIB, *host_objs, "-lm"], verbose)
     refabi_src = os.path.join(HOST, "csem_refabi.c")
     if force or _newer(REFABI, [refabi_src, LIB] + hdrs):
         _run(["gcc", "-O3", "-fPIC", "-ffp-contract=off", "-std=gnu99", "-Wall", "-shared", "-I", INCLUDE, refabi_src,

@@ -121,6 +121,53 @@ class _Desc(C.Structure):
                 ("jx", _ip), ("jy", _ip), ("wx", _dp), ("wy", _dp)]
 
 
+def setup_grid(d: str, params: dict) -> GridArrays:
+    """The padded model of a case directory (fx1..3, frho11..33) for the oracle, through
+    the host set-up library alone (libcsem_host.so: csem_grid_read / extend / airbc, the
+    restatement of extend_model.c, create_nugrid.c, find_index.c and airbc_init_free.c:24-109
+    that tests/test_oracle_golden.py pins bit for bit to the reference; no CUDA is loaded)."""
+    import sys
+    root = os.path.dirname(HERE)
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    from demo_matrixfree_csem_gb300 import build as pbuild
+    from demo_matrixfree_csem_gb300.api import _Grid
+    if not os.path.exists(pbuild.HOST_LIB):
+        pbuild.build()
+    L = C.CDLL(pbuild.HOST_LIB)
+    L.csem_last_error.restype = C.c_char_p
+    g = _Grid()
+    names = [os.path.join(d, n).encode() for n in ("fx1", "fx2", "fx3", "frho11", "frho22", "frho33")]
+    if L.csem_grid_read(C.byref(g), *names):
+        raise RuntimeError(L.csem_last_error().decode())
+    if L.csem_grid_extend(C.byref(g), int(params.get("nb", 15)), C.c_float(float(params.get("lextend", -1))),
+                          C.c_float(float(params.get("rho_air", 1e6))), int(params.get("istretch", 1))):
+        raise RuntimeError(L.csem_last_error().decode())
+    airbc = int(params.get("airbc", 0))
+    if airbc and L.csem_grid_airbc(C.byref(g), int(params.get("n1fft", 1024)), int(params.get("n2fft", 1024))):
+        raise RuntimeError(L.csem_last_error().decode())
+    n1, n2, n3 = g.n1, g.n2, g.n3
+
+    def a(name, n, dtype=np.float64):
+        return np.ctypeslib.as_array(getattr(g, name), (n,)).astype(dtype, copy=True)
+
+    kw = {}
+    if airbc:
+        N = g.n1fft * g.n2fft
+        kw = dict(n1fft=g.n1fft, n2fft=g.n2fft, d1fft=g.d1fft, d2fft=g.d2fft,
+                  sH1=a("sH1", 2 * N).view(np.complex128), sH2=a("sH2", 2 * N).view(np.complex128),
+                  jx=a("jx", g.n1fft, np.int32), jy=a("jy", g.n2fft, np.int32), wx=a("wx", g.n1fft),
+                  wy=a("wy", g.n2fft))
+    out = GridArrays(n1, n2, n3, g.nb, g.nz, airbc, int(params.get("fvm", 0)),
+                     *[a(nm, ln) for nm, ln in (("x1", n1 + 1), ("x2", n2 + 1), ("x3", n3 + 1), ("x1s", n1 + 1),
+                                                ("x2s", n2 + 1), ("x3s", n3 + 1), ("d1", n1 + 1), ("d2", n2 + 1),
+                                                ("d3", n3 + 1), ("d1s", n1 + 1), ("d2s", n2 + 1), ("d3s", n3 + 1))],
+                     a("sigma11", n1 * (n2 + 1) * (n3 + 1)), a("sigma22", (n1 + 1) * n2 * (n3 + 1)),
+                     a("sigma33", (n1 + 1) * (n2 + 1) * n3), rho_water=float(g.rho_water), **kw)
+    L.csem_grid_free(C.byref(g))
+    return out
+
+
 class Oracle:
     """The C restatement of the reference's hot path (oracle/csem_oracle.c)."""
 

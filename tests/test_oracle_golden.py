@@ -59,3 +59,29 @@ def test_oracle_solver_bit_exact(case):
     rec = read_rows(f"{d}/receivers.txt")
     out = O.extract(channels(p, "chrec"), rec, x)
     assert np.array_equal(out.astype(np.complex64), gold["dcal"])
+
+
+def test_host_setup_matches_reference_at_bench_scale(tmp_path):
+    """The product's set-up of the 96-system bench model (nb=10 stretched padding to
+    120 km, the bottom-padding quirk of extend_model.c:169-173, 1024x1024 airwave
+    filters) is bit-identical to the reference's: every array hashes to the checksum the
+    reference's own set-up produced (tests/golden/make_setup_checksums.py). The oracle
+    takes its model from the same host set-up library (oracle.pyoracle.setup_grid)."""
+    import hashlib
+    import json
+    import os
+
+    from cases import GOLDEN
+    from demo_matrixfree_csem_gb300 import synthetic
+    from oracle.pyoracle import setup_grid
+    want = json.load(open(os.path.join(GOLDEN, "marlim_like_96", "setup_sha256.json")))
+    cfg = synthetic.workload("marlim_like_96")
+    synthetic.write_config(cfg, str(tmp_path))
+    g = setup_grid(str(tmp_path), {k: str(v) for k, v in cfg.params.items()})
+    assert (g.n1, g.n2, g.n3f, g.nb, g.n1fft, g.n2fft) == (want["n1"], want["n2"], want["n3"], want["nb"],
+                                                          want["n1fft"], want["n2fft"])
+    nv = want["valid_airwave_nodes"]  # the reference leaves the nodes past the model unwritten
+    got = {k: hashlib.sha256(np.ascontiguousarray(getattr(g, k)[:nv[k]] if k in nv else getattr(g, k)).tobytes())
+           .hexdigest() for k in want["sha256"]}
+    bad = [k for k in want["sha256"] if got[k] != want["sha256"][k]]
+    assert not bad, bad
