@@ -12,17 +12,26 @@ frequencies) to convergence, injection and receiver extraction included; steps w
 48 measured 7% more solves/s than waves of 16 (fewer steps in which only a few slow
 systems keep the GPU busy); waves of all 96 a further 2%, at twice the time per step.
 
-  value  solves/s with the model resident on the GPU, timed with CUDA events on the
-         solver's stream over exactly K steps (synchronize + barrier on both sides);
-  e2e    the same through the C ABI call a user makes (csem_solve_batch_host) with host
-         (pinned) buffers for the per-step inputs (frequencies, source and receiver
-         positions, channel lists) and outputs (receivers), timed on the host clock.
+  value     solves/s with the model resident on the GPU, timed with CUDA events on the
+            solver's stream over exactly K steps (synchronize + barrier on both sides),
+            with the product defaults (CUDA-graph replay of the inner iterations);
+  e2e       the same through the C ABI call a user makes (csem_solve_batch_host) with
+            host (pinned) buffers for the per-step inputs (frequencies, source and
+            receiver positions, channel lists) and outputs (receivers), host clock;
+  roofline  the dominant operator's algorithmic bytes per application over its average
+            duration, from CUDA events around every application during one profiled
+            wave (the last warm-up wave; profiling replaces graph replay by direct
+            launches, so it is kept out of the timed steps);
+  accuracy  max-norm relative receiver error per frequency and channel of the timed
+            systems that tests/golden/marlim_like_96/fp64_receivers.npz also holds
+            (complex128 solves of all six frequencies x sources 0, 7, 15).
 
 `--impl reference` times the reference's CPU implementation of the path instead (the
 compiled reference when its sources are present, else the C restatement in oracle/) on
 all host cores: one process per core, each timing a bounded number of iterations of one
-system, extrapolated to whole solves with the reference's published Marlim iteration
-counts (run_marlim/out.txt: 1000, 1000, 915, 696, 463, 354 iterations at 0.125-1.25 Hz).
+system; solves/s are extrapolated with the reference's own iteration counts on this
+model (tests/golden/marlim_like_96/reference_receivers.npz: its BiCGStab + LU-SGS at
+niter=1000 takes 1000, 1000, 641, 468, 391, 317 iterations at 0.125-1.25 Hz).
 """
 from __future__ import annotations
 
@@ -40,7 +49,26 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-MARLIM_ITERS = {0.125: 1000, 0.25: 1000, 0.5: 915, 0.75: 696, 1.0: 463, 1.25: 354}
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def reference_iterations(workload: str) -> dict:
+    """Iterations the reference itself takes per frequency on this workload (its
+    residual history holds one entry per iteration plus the initial one while it
+    converges, and exactly niter entries when it stops at niter)."""
+    path = os.path.join(GOLDEN, workload, "reference_receivers.npz")
+    z = np.load(path)
+    out = {}
+    for f in range(len(z["freqs"])):
+        n = len(z[f"hist{f}"])
+        out[round(float(z["freqs"][f]), 4)] = n if n >= 1000 else n - 1
+    return out
+
+
+def complex128_iterations(workload: str) -> list:
+    """Iterations of the complex128 GPU solver on the systems of fp64_receivers.npz."""
+    path = os.path.join(GOLDEN, workload, "fp64_receivers.npz")
+    return [int(v) for v in np.load(path)["iters"]] if os.path.exists(path) else []
 
 
 def log(*a):
@@ -114,10 +142,8 @@ if {use_ref!r}:
     ifreq = [float(f) for f in R.freqs].index(min(R.freqs, key=lambda f: abs(f - {freq})))
     x, b, t = R.solve(ifreq, niter={iters})
 else:
-    from cases import oracle_for, product_grid
-    p = {{k: str(v) for k, v in cfg.params.items()}}
-    G = product_grid(d, p)
-    O = oracle_for(G, p)
+    from oracle.pyoracle import Oracle, setup_grid
+    O = Oracle(setup_grid(d, {{k: str(v) for k, v in cfg.params.items()}}))
     O.set_freq({freq})
     b = O.inject([0], cfg.acq.src[0])
     t0 = time.perf_counter()
@@ -134,6 +160,9 @@ print("SECONDS", t)
 
 
 def cpu_baseline(workload: str, freqs, processes: int, iters: int):
+    """solves/s of the reference's CPU path on `processes` host cores: each process
+    times `iters` FBiCGStab + LU-SGS iterations of one system of the workload; a whole
+    solve takes the reference's own iteration count on this workload at each frequency."""
     import oracle
     use_ref = oracle.ref_available() and os.path.exists(oracle.build_ref() or "")
     oracle.build_oracle()
@@ -147,13 +176,16 @@ def cpu_baseline(workload: str, freqs, processes: int, iters: int):
             spi = list(ex.map(lambda _: cpu_sample(workload, fmid, iters, use_ref), range(processes)))
     wall = time.perf_counter() - t0
     s_it = statistics.mean(spi)
-    its = statistics.mean(MARLIM_ITERS.get(round(f, 3), 700) for f in freqs)
+    ref_its = reference_iterations(workload)
+    its = statistics.mean(ref_its[round(f, 4)] for f in freqs)
     solves_per_s = processes / (s_it * its)
     return {"value": solves_per_s, "unit": "solves/s", "cores": processes,
             "kind": "reference" if use_ref else "port",
             "sample": (f"{processes} process(es) x {iters} FBiCGStab+LU-SGS iterations of one {workload} system at "
-                       f"{fmid} Hz ({s_it:.3f} s/iteration, {wall:.1f} s wall); extrapolated with the reference's "
-                       f"published Marlim iteration counts (mean {its:.0f} iterations per solve)")}
+                       f"{fmid} Hz ({s_it:.3f} s/iteration, {wall:.1f} s wall); a whole solve taken as the "
+                       f"reference's own iteration count on this model (mean {its:.0f} over the frequencies: "
+                       + "/".join(str(ref_its[round(f, 4)]) for f in freqs) + ")"),
+            "sample_wall_s": wall, "seconds_per_iteration": s_it, "iterations_per_solve": its}
 
 
 # ----------------------------------------------------------------------------- ranks
@@ -171,6 +203,13 @@ def wave_systems(cfg, systems, wave, k, rank):
     return f, src
 
 
+def wave_sources(systems, wave, k):
+    """Source indices of the systems of step k, in wave order."""
+    nwaves = (len(systems) + wave - 1) // wave
+    w = k % nwaves
+    return [s[1] for s in systems[w * wave:(w + 1) * wave]]
+
+
 def max_over_ranks(values, device):
     """Element-wise maximum over all ranks of a list of floats (the timed region of the
     slowest rank)."""
@@ -182,28 +221,62 @@ def max_over_ranks(values, device):
 
 
 # ----------------------------------------------------------------------------- FP64 drop-in leg
-def fp64_dropin(ctx, cfg, freqs, iters: int):
-    """The plain complex128 GPU drop-in (csem_solve_fp64_host: BiCGStab + LU-SGS, the
-    reference's arithmetic) on one system of the workload: seconds per iteration from
-    CUDA events on the solver's stream, extrapolated to whole solves with the same
-    published Marlim iteration counts as the CPU legs."""
+def fp64_dropin(ctx, cfg, freqs):
+    """The plain complex128 GPU drop-in (csem_solve_fp64_host: BiCGStab + LU-SGS with the
+    reference's arithmetic, one system at a time, as the reference's driver) on one whole
+    system of the workload: source 0 at the highest frequency, solved to convergence and
+    timed on the host around the call (upload, solve, download). Solves/s of the whole
+    workload take that measured time per iteration and the complex128 solver's own
+    iteration counts on the 18 systems of fp64_receivers.npz (all six frequencies)."""
     import demo_matrixfree_csem_gb300 as cs
     import torch
-    fmid = 0.5 if 0.5 in freqs else freqs[len(freqs) // 2]
-    iom = cs.iom_of(fmid)
+    f = max(freqs)
+    iom = cs.iom_of(f)
     b = ctx.inject_source(iom, ["Ex"], cfg.acq.src[0])
-    st = torch.cuda.ExternalStream(ctx.stream)
+    tol = float(np.float32(np.float32(1e-8) / np.float32(f)))
     ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=2, tol=1e-30)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=iters, tol=1e-30)
+    _, _, it, st = ctx.solve_fp64(iom, b, algopt=1, preco=1, niter=4000, tol=tol)
     torch.cuda.synchronize()
-    s_it = (time.perf_counter() - t0) / iters
-    its = statistics.mean(MARLIM_ITERS.get(round(f, 3), 700) for f in freqs)
-    return {"value": 1.0 / (s_it * its), "unit": "solves/s", "s_per_iteration": s_it, "iterations_per_solve": its,
-            "sample": (f"{iters} complex128 BiCGStab+LU-SGS iterations of one {cfg.name} system at {fmid} Hz through "
-                       f"csem_solve_fp64_host (upload, solve, download); extrapolated with the reference's published "
-                       f"Marlim iteration counts (mean {its:.0f} per solve)")}
+    wall = time.perf_counter() - t0
+    s_it = wall / max(it, 1)
+    its = complex128_iterations(cfg.name + "_96" if cfg.name == "marlim_like" else cfg.name)
+    mean_its = statistics.mean(its) if its else float(it)
+    return {"value": 1.0 / (s_it * mean_its), "unit": "solves/s", "s_per_iteration": s_it,
+            "measured_solve": {"freq": f, "iterations": it, "status": st, "seconds": wall},
+            "iterations_per_solve": mean_its,
+            "sample": (f"one whole complex128 BiCGStab+LU-SGS solve of a {cfg.name} system at {f} Hz through "
+                       f"csem_solve_fp64_host ({it} iterations, {wall:.1f} s); per solve the mean complex128 "
+                       f"iteration count of {len(its)} systems at all six frequencies ({mean_its:.0f})")}
+
+
+def accuracy(cfg, dcal_by_system):
+    """Max-norm relative receiver error per frequency and channel against the complex128
+    receivers of fp64_receivers.npz, over the timed systems that file holds."""
+    path = os.path.join(GOLDEN, "marlim_like_96", "fp64_receivers.npz")
+    if cfg.name != "marlim_like" or not os.path.exists(path):
+        return None
+    z = np.load(path)
+    per = {}
+    n = 0
+    for q in range(len(z["freqs"])):
+        key = (round(float(z["freqs"][q]), 4), int(z["isrc"][q]))
+        if key not in dcal_by_system:
+            continue
+        got, ref = dcal_by_system[key], z["rec"][q]
+        ex = np.abs(ref[0]).max()
+        err = [float(np.abs(got[c] - ref[c]).max() / (np.abs(ref[c]).max() if c != 1 else ex)) for c in range(3)]
+        f = str(key[0])
+        per[f] = [max(a, b) for a, b in zip(per.get(f, [0.0] * 3), err)]
+        n += 1
+    if not n:
+        return None
+    return {"vs": "complex128 GPU solver (reference arithmetic, converged to 1e-8/f), "
+                  "tests/golden/marlim_like_96/fp64_receivers.npz",
+            "metric": "max-norm relative error over the receiver line; Ey against the Ex maximum",
+            "channels": ["Ex", "Ey", "Ez"], "per_frequency": per, "systems": n,
+            "worst": max(max(v) for v in per.values()), "target": 1e-7}
 
 
 # ----------------------------------------------------------------------------- GPU leg
@@ -239,19 +312,29 @@ def run_ours(args):
         pin[id(t)] = t
         return t.numpy()
 
+    for name, v in args.ctx_options.items():
+        ctx.set_option(name, v)
     log(f"[bench] {args.workload}: {len(systems)} systems, waves of {wave}, lE={ctx.lE}")
+    prof = None
     for k in range(args.warmup):
         f, s = step_systems(k)
+        last = k == args.warmup - 1
+        if last:  # per-operator CUDA events for the roofline, outside the timed steps
+            cs.profile(True)
         cs.solve_batch(ctx, f, s, **opts)
+        if last:
+            torch.cuda.synchronize()
+            prof = cs.profile_read()
+            cs.profile(False)
     torch.cuda.synchronize()
     if dist:
         tdist.barrier()
     clocks = ClockSampler(local)
-    cs.profile(True)
     l0 = cs.api.launch_count()
     nsolved = 0
     iters = []
     stat = []
+    dcal = {}
     solver_stream = torch.cuda.ExternalStream(ctx.stream)  # the stream every solver kernel runs on
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -269,13 +352,14 @@ def run_ours(args):
         nsolved += len(f)
         iters += r["iters"].tolist()
         stat += r["status"]
+        if rank == 0:
+            for q, isrc in enumerate(wave_sources(systems, wave, k)):
+                dcal[(round(float(f[q]), 4), isrc)] = r["dcal"][q]
     torch.cuda.synchronize()
     if dist:
         tdist.barrier()
     wall = time.perf_counter() - t0
     launches = cs.api.launch_count() - l0
-    prof = cs.profile_read()
-    cs.profile(False)
     ck = clocks.stop()
     if dist:
         wall, dev_s = max_over_ranks([wall, dev_ms / 1e3], "cuda")
@@ -283,9 +367,10 @@ def run_ours(args):
     else:
         dev_s = dev_ms / 1e3
     result = dict(wall=wall, dev_s=dev_s, nsolved=nsolved, iters=iters, status=stat, prof=prof, launches=launches,
-                  clocks=ck, lE=ctx.lE, n1=ctx.n1, n2=ctx.n2, n3=ctx.n3, n3f=ctx.n3f, world=world, rank=rank)
-    if args.fp64_iters > 0 and rank == 0:
-        result["fp64"] = fp64_dropin(ctx, cfg, freqs, args.fp64_iters)
+                  clocks=ck, lE=ctx.lE, n1=ctx.n1, n2=ctx.n2, n3=ctx.n3, n3f=ctx.n3f, world=world, rank=rank,
+                  accuracy=accuracy(cfg, dcal) if rank == 0 else None)
+    if args.fp64 and rank == 0:
+        result["fp64"] = fp64_dropin(ctx, cfg, freqs)
     return result, cfg, freqs, systems
 
 
@@ -348,10 +433,13 @@ def main():
                     help="inner iteration budget per system (the reference's niter); lower values are for "
                          "profiling runs, whose systems then stop unconverged")
     ap.add_argument("--max-outer", type=int, default=30, help="defect-correction cycles per system")
-    ap.add_argument("--fp64-iters", type=int, default=8,
-                    help="iterations of the complex128 drop-in timed for the fp64_dropin comparison (0: skip)")
+    ap.add_argument("--no-fp64", dest="fp64", action="store_false",
+                    help="skip the whole complex128 drop-in solve of the fp64_dropin comparison")
+    ap.add_argument("--ctx-option", action="append", default=[], metavar="NAME=VALUE",
+                    help="a csem_ctx_set_option for the solver context (repeatable)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    args.ctx_options = {kv.split("=", 1)[0]: int(kv.split("=", 1)[1]) for kv in args.ctx_option}
     rank = int(os.environ.get("RANK", 0))
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -369,9 +457,12 @@ def main():
         cb = dict(samples[-1])
         cb["value"] = statistics.mean(x["value"] for x in samples)
         cb["sample"] = f"mean of {len(samples)} steps, each: " + cb["sample"]
+        step_ms = 1e3 * statistics.mean(x["sample_wall_s"] for x in samples)
         line = {"impl": "reference", "metric": metric, "value": cb["value"], "unit": "solves/s",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": 1e3 * args.wave / cb["value"], "higher_is_better": True, "scaling": "weak",
+                "ms_per_step": step_ms, "ms_per_step_is": "wall time of one measured sample (all host cores)",
+                "extrapolated_ms_per_wave": 1e3 * args.wave / cb["value"], "higher_is_better": True,
+                "scaling": "weak",
                 "vs_baseline": None, "dtype": "c128", "data": "synthetic",
                 "config": {"workload": args.workload, "systems": len(systems), "wave": args.wave},
                 "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "solves/s", "h2d_bytes_per_step": 0,
@@ -394,9 +485,12 @@ def main():
         "config": {"workload": args.workload, "systems": len(systems), "wave": args.wave, "grid": [res["n1"], res["n2"], res["n3"]],
                    "unknowns_per_system": res["lE"], "solver": "FBiCGStab+LU-SGS complex64 inner, complex128 defect correction",
                    "tol": "1e-8/f", "airbc": 1, "l2": "working set >> L2 (inputs larger than L2)",
-                   "inner_tol": args.inner_tol},
+                   "inner_tol": args.inner_tol, "options": args.ctx_options},
         "roofline": rf[dom] | {"kernel": dom},
         "roofline_all": rf,
+        "roofline_source": "CUDA events on the solver stream around every operator application of the last "
+                           "warm-up wave (direct launches); the timed steps replay CUDA graphs",
+        "accuracy": res["accuracy"],
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],

@@ -3,6 +3,7 @@ reads, and the waves the default configuration walks."""
 import os
 import sys
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -53,3 +54,44 @@ def test_default_waves_cover_the_batch_once():
         assert len(f) == 48 and src.shape == (48, 3)
         seen += [(float(a), tuple(b)) for a, b in zip(f, src)]
     assert len(set(seen)) == 96
+
+
+def test_reference_iteration_counts_come_from_the_reference_run():
+    """The CPU legs extrapolate with the reference's own iteration counts on the bench
+    model (its committed residual histories), not with published figures of another run."""
+    import bench
+    its = bench.reference_iterations("marlim_like_96")
+    assert [its[f] for f in (0.125, 0.25, 0.5, 0.75, 1.0, 1.25)] == [1000, 1000, 641, 468, 391, 317]
+    c128 = bench.complex128_iterations("marlim_like_96")
+    assert len(c128) == 18 and all(v > 0 for v in c128)
+
+
+def test_accuracy_field_flags_a_planted_error():
+    """accuracy() compares the timed systems the complex128 fixture holds, per frequency
+    and channel; an error planted in one receiver of one system shows up there and only
+    there."""
+    import bench
+    from demo_matrixfree_csem_gb300 import synthetic
+    z = np.load(os.path.join(bench.GOLDEN, "marlim_like_96", "fp64_receivers.npz"))
+    cfg = synthetic.workload("marlim_like_96")
+    dcal = {(round(float(z["freqs"][q]), 4), int(z["isrc"][q])): z["rec"][q].copy() for q in range(len(z["freqs"]))}
+    a = bench.accuracy(cfg, dcal)
+    assert a["systems"] == 18 and a["worst"] == 0.0
+    key = (0.25, 7)
+    r = int(np.argmax(np.abs(dcal[key][2])))
+    dcal[key][2, r] *= 1 + 3e-6
+    a = bench.accuracy(cfg, dcal)
+    assert a["per_frequency"]["0.25"][2] > 1e-7 and a["per_frequency"]["0.25"][0] == 0.0
+    assert all(max(v) == 0.0 for f, v in a["per_frequency"].items() if f != "0.25")
+
+
+def test_wave_sources_follow_wave_systems():
+    import bench
+    from demo_matrixfree_csem_gb300 import synthetic
+    cfg = synthetic.workload("marlim_like_96")
+    freqs = [float(f) for f in cfg.params["freqs"].split(",")]
+    systems = [(f, s) for f in freqs for s in range(len(cfg.acq.src))]
+    for k in range(3):
+        f, src = bench.wave_systems(cfg, systems, 48, k, 0)
+        idx = bench.wave_sources(systems, 48, k)
+        assert np.array_equal(src, cfg.acq.src[idx, :3])
