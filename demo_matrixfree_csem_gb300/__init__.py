@@ -7,4 +7,5 @@ layer in C that keeps the reference's key=value driver, float32 model files and
 emf_NNNN.txt output, and Python bindings (api.py).
 """
 from .api import (CHANNELS, STATUS, CsemError, Ctx, Grid, cdot, device_count, iom_of,  # noqa: F401
-                  launch_count, lib, profile, profile_read, solve_batch, solve_batches)
+                  launch_count, lib, partition_systems, profile, profile_read, solve_batch,
+                  solve_batch_multi, solve_batches)

@@ -89,6 +89,10 @@ def lib(build_if_missing: bool = True):
         "csem_ctx_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
         "csem_batch_bytes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp]),
         "csem_solve_batches_host": (C.c_int, [C.c_int, C.c_void_p]),
+        "csem_partition_systems": (C.c_int, [C.c_int, _fp, _dp, C.c_double, C.c_int, _ip, _dp]),
+        "csem_solve_batch_multi": (C.c_int, [C.c_int, _ip, C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, C.c_int,
+                                             _ip, C.c_int, _ip, C.c_int, _fp, C.c_void_p, _dp, _ip, _ip, _ip, _dp,
+                                             _ip]),
         "csem_batch_capacity": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _ip]),
         "csem_fdfd_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
         "csem_lusgs_apply_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _dp, _dp]),
@@ -372,6 +376,45 @@ def solve_batch(ctx: Ctx, freqs, srcs, chsrc=("Ex",), chrec=("Ex", "Ey", "Ez"), 
                                        _p(cr, _ip), len(r), _p(r, _fp), C.byref(o), _p(dcal.view(np.float64)),
                                        _p(it, _ip), _p(ou, _ip), _p(st, _ip), _p(rr)))
     return dict(dcal=dcal, iters=it, outer=ou, status=[STATUS.get(int(v), int(v)) for v in st], relres=rr)
+
+
+def partition_systems(ndev: int, freqs=None, cost=None, unknowns: float = 1.0):
+    """Balanced split of systems over ndev devices (csem_partition_systems): returns
+    (owner slot per system, summed work per slot). Work is cost[s] when given, else
+    unknowns * freqs[s]^(-2/3)."""
+    f = np.ascontiguousarray(freqs if freqs is not None else np.zeros(0), np.float32)
+    c = None if cost is None else np.ascontiguousarray(cost, np.float64)
+    n = len(c) if c is not None else len(f)
+    owner = np.zeros(n, np.int32)
+    load = np.zeros(ndev)
+    _check(lib().csem_partition_systems(n, _p(f, _fp) if len(f) else None, _p(c) if c is not None else None,
+                                        float(unknowns), int(ndev), _p(owner, _ip), _p(load)))
+    return owner, load
+
+
+def solve_batch_multi(grid: "Grid", devices, freqs, srcs, airbc=0, fvm=0, chsrc=("Ex",), chrec=("Ex", "Ey", "Ez"),
+                      rec=None, precision=32, algopt=1, preco=1, niter=1000, tol=1e-8, inner_tol=0.2, check_every=4,
+                      max_outer=30, nrestart=10, mp=30):
+    """Solve the systems of one model on several devices (csem_solve_batch_multi): one
+    context and host thread per entry of `devices`, the systems split by
+    partition_systems, outputs gathered in the original order. Returns solve_batch's
+    dict plus 'owner' (slot of each system)."""
+    f = np.ascontiguousarray(freqs, np.float32)
+    s = np.ascontiguousarray(np.asarray(srcs, np.float32)[:, :3])
+    nsys = len(f)
+    dv = np.ascontiguousarray(devices, np.int32)
+    cs_ = np.asarray([CHANNELS[c] if isinstance(c, str) else c for c in chsrc], np.int32)
+    cr = np.asarray([CHANNELS[c] if isinstance(c, str) else c for c in chrec], np.int32)
+    r = np.ascontiguousarray(rec if rec is not None else np.zeros((0, 5)), np.float32)
+    o = _BatchOpts(precision, algopt, preco, niter, tol, inner_tol, check_every, max_outer, nrestart, mp)
+    dcal = np.zeros((nsys, len(cr), len(r)), np.complex128)
+    it, ou, st, own = (np.zeros(nsys, np.int32) for _ in range(4))
+    rr = np.zeros(nsys)
+    _check(lib().csem_solve_batch_multi(len(dv), _p(dv, _ip), C.byref(grid.g), airbc, fvm, nsys, _p(f, _fp),
+                                        _p(s, _fp), len(cs_), _p(cs_, _ip), len(cr), _p(cr, _ip), len(r), _p(r, _fp),
+                                        C.byref(o), _p(dcal.view(np.float64)), _p(it, _ip), _p(ou, _ip), _p(st, _ip),
+                                        _p(rr), _p(own, _ip)))
+    return dict(dcal=dcal, iters=it, outer=ou, status=[STATUS.get(int(v), int(v)) for v in st], relres=rr, owner=own)
 
 
 class _BatchJob(C.Structure):

@@ -31,7 +31,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["k_fdfd.cu", "k_airwave.cu", "k_lusgs.cu", "k_lusgs2.cu", "k_lusgs3.cu", "k_blas.cu", "k_scalar.cu", "k_acq.cu",
               "engine_model.cu", "solve_fp64.cu", "solve_mixed.cu", "prof.cu", "capi.cu", "capi_noalloc.cu",
               "csr_compare.cu"]
-C_SOURCES = ["csem_getpar.c", "csem_setup.c"]
+C_SOURCES = ["csem_getpar.c", "csem_setup.c", "csem_partition.c"]
 DRIVER_SOURCES = ["csem_main.c"]
 
 

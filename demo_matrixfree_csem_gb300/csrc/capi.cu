@@ -277,6 +277,82 @@ int csem_solve_batches_host(int njobs, csem_batch_job* jobs)
   return CSEM_OK;
 }
 
+int csem_solve_batch_multi(int ndev, const int* devices, const csem_grid_t* g, int airbc, int fvm, int nsys,
+                           const float* freq, const float* src3, int nchsrc, const int* chsrc, int nchrec,
+                           const int* chrec, int nrec, const float* rec, const csem_batch_opts* opt, double* dcal,
+                           int* iters, int* outer, int* status, double* relres, int* owner)
+{
+  if (ndev < 1 || !devices || !g || nsys < 1 || !freq || !src3 || !opt || !dcal)
+    return csem_set_error(CSEM_EINVAL, "csem_solve_batch_multi: bad arguments");
+  const int ndevs = csem_device_count();
+  if (ndevs < 1) return csem_set_error(CSEM_ENODEV, "no CUDA device available");
+  for (int d = 0; d < ndev; d++)
+    if (devices[d] < 0 || devices[d] >= ndevs)
+      return csem_set_error(CSEM_EINVAL, "csem_solve_batch_multi: device %d does not exist", devices[d]);
+  // work per system: unknowns of the operator grid (the same model on every slot)
+  const long n3 = airbc ? (long)g->nz + g->nb : (long)g->n3;
+  const double unknowns = (double)g->n1 * (g->n2 + 1) * (n3 + 1) + (double)(g->n1 + 1) * g->n2 * (n3 + 1) +
+                          (double)(g->n1 + 1) * (g->n2 + 1) * n3;
+  std::vector<int> own(nsys);
+  int rc = csem_partition_systems(nsys, freq, nullptr, unknowns, ndev, own.data(), nullptr);
+  if (rc) return rc;
+  if (owner)
+    for (int s = 0; s < nsys; s++) owner[s] = own[s];
+  const size_t per = (size_t)nchrec * (nrec > 0 ? nrec : 0) * 2;
+  std::vector<int> rcs(ndev, CSEM_OK);
+  std::vector<std::string> msgs(ndev);
+  auto run = [&](int d) {
+    std::vector<int> mine;
+    for (int s = 0; s < nsys; s++)
+      if (own[s] == d) mine.push_back(s);
+    if (mine.empty()) return;
+    const int m = (int)mine.size();
+    std::vector<float> f(m), xyz(3 * (size_t)m);
+    for (int q = 0; q < m; q++) {
+      f[q] = freq[mine[q]];
+      for (int c = 0; c < 3; c++) xyz[3 * (size_t)q + c] = src3[3 * (size_t)mine[q] + c];
+    }
+    std::vector<double> dc(per * m + 1), rr(m);
+    std::vector<int> it(m), ou(m), st(m);
+    csem_ctx* ctx = nullptr;
+    int r = cudaSetDevice(devices[d]) == cudaSuccess ? CSEM_OK
+                                                      : csem_set_error(CSEM_ECUDA, "cudaSetDevice(%d) failed", devices[d]);
+    if (!r) r = csem_ctx_create(g, airbc, fvm, &ctx);
+    if (!r)
+      r = csem_solve_batch_host(ctx, m, f.data(), xyz.data(), nchsrc, chsrc, nchrec, chrec, nrec, rec, opt,
+                                dc.data(), it.data(), ou.data(), st.data(), rr.data());
+    if (ctx) csem_ctx_destroy(ctx);
+    if (r) {
+      rcs[d] = r;
+      msgs[d] = csem_last_error();  // the message lives in this thread
+      return;
+    }
+    for (int q = 0; q < m; q++) {  // the gather: this slot's systems at their positions
+      const int s = mine[q];
+      for (size_t k = 0; k < per; k++) dcal[per * (size_t)s + k] = dc[per * (size_t)q + k];
+      if (iters) iters[s] = it[q];
+      if (outer) outer[s] = ou[q];
+      if (status) status[s] = st[q];
+      if (relres) relres[s] = rr[q];
+    }
+  };
+  int caller_dev = 0;
+  cudaGetDevice(&caller_dev);
+  std::vector<std::thread> th;
+  try {
+    for (int d = 1; d < ndev; d++) th.emplace_back(run, d);
+  } catch (const std::system_error&) {
+    for (auto& t : th) t.join();
+    return csem_set_error(CSEM_ENOMEM, "csem_solve_batch_multi: cannot start threads");
+  }
+  run(0);
+  for (auto& t : th) t.join();
+  cudaSetDevice(caller_dev);  // slot 0 ran on this thread
+  for (int d = 0; d < ndev; d++)
+    if (rcs[d]) return csem_set_error(rcs[d], "slot %d (device %d): %s", d, devices[d], msgs[d].c_str());
+  return CSEM_OK;
+}
+
 int csem_ctx_sync(csem_ctx* c)
 {
   API_BEGIN

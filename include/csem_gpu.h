@@ -152,6 +152,21 @@ typedef struct csem_batch_job {
 } csem_batch_job;
 int csem_solve_batches_host(int njobs, csem_batch_job *jobs);
 
+/* ------------------------------------------------------------ systems over several GPUs
+ * Solve nsys systems of one model on ndev devices: csem_partition_systems splits them
+ * (work = unknowns x freq^(-2/3)), every slot d gets its own context on CUDA device
+ * devices[d] (model upload, stream, workspaces) driven by its own host thread through
+ * csem_solve_batch_host, and each slot writes its systems' outputs at their original
+ * positions in the caller's arrays: the only gather is these host writes, with no
+ * communication between the GPUs. owner (may be NULL) receives each system's slot.
+ * The same device may be named by several slots (independent contexts share it).
+ * The reference solves one system per process (main.c:93-123). Returns CSEM_OK, or the
+ * code of the first slot that failed (with that slot's message). */
+int csem_solve_batch_multi(int ndev, const int *devices, const csem_grid_t *g, int airbc, int fvm, int nsys,
+                           const float *freq, const float *src3, int nchsrc, const int *chsrc, int nchrec,
+                           const int *chrec, int nrec, const float *rec, const csem_batch_opts *opt, double *dcal,
+                           int *iters, int *outer, int *status, double *relres, int *owner);
+
 /* Capacity planning for large sets of systems (no counterpart in the reference, which
  * solves one system at a time). csem_batch_bytes: device bytes csem_solve_batch_host
  * needs for nsys systems with this precision and preconditioner, beyond the model and

@@ -127,6 +127,21 @@ int csem_write_emf(const char *fname, int isrc, int nchrec, int nfreq, int nrec,
  * comparator on the float bit patterns, emf_init_free.c:12,27). */
 void csem_sort_freqs(float *freqs, int n);
 
+/* ---------------------------------------------------------------- systems over GPUs ---
+ * Split nsys independent systems over ndev devices so that the expected work per device
+ * is balanced. No counterpart in the reference, which solves one system per process
+ * (main.c:93-123; its acquisition keeps only the first source, acq_init_free.c:56,90).
+ * The work of system s is cost[s] when cost is given; otherwise unknowns * freq[s]^(-2/3):
+ * BiCGStab + LU-SGS iteration counts fall with frequency about as f^(-2/3) on the bench
+ * model (the complex128 solver needs 1521, 987, 633, 423, 338 and 327 iterations at
+ * 0.125, 0.25, 0.5, 0.75, 1.0 and 1.25 Hz for its first source). Longest work first:
+ * systems in decreasing work (ties: lower index first) each go to the device with the
+ * least work so far (ties: lower slot), so the split is deterministic. owner[s] receives
+ * the slot 0..ndev-1 of system s; load (may be NULL) the summed work per slot.
+ * CSEM_EINVAL for ndev < 1, nsys < 0, missing arrays or non-positive work. */
+int csem_partition_systems(int nsys, const float *freq, const double *cost, double unknowns, int ndev, int *owner,
+                           double *load);
+
 #ifdef __cplusplus
 }
 #endif

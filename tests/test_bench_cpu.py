@@ -41,16 +41,18 @@ def test_roofline_arithmetic():
     assert bench.roofline(res, {})[1]["lusgs32"]["traffic"] is None
 
 
-def test_default_waves_cover_the_batch_once():
+def test_default_waves_cover_the_batch_once(csem_lib):
     import bench
     from demo_matrixfree_csem_gb300 import synthetic
     cfg = synthetic.workload("marlim_like_96")  # the model in memory; nothing written
     freqs = [float(f) for f in cfg.params["freqs"].split(",")]
     systems = [(f, s) for f in freqs for s in range(len(cfg.acq.src))]
     assert len(systems) == 96 and len(freqs) == 6
+    mine = bench.rank_systems(systems, 1, 0, 11064870)
+    assert [(f, s) for f, s, r in mine] == systems  # one rank: the workload in its own order
     seen = []
     for k in range(2):  # the default: 2 timed steps of 48
-        f, src = bench.wave_systems(cfg, systems, 48, k, 0)
+        f, src = bench.wave_systems(cfg, mine, 48, k)
         assert len(f) == 48 and src.shape == (48, 3)
         seen += [(float(a), tuple(b)) for a, b in zip(f, src)]
     assert len(set(seen)) == 96
@@ -85,13 +87,16 @@ def test_accuracy_field_flags_a_planted_error():
     assert all(max(v) == 0.0 for f, v in a["per_frequency"].items() if f != "0.25")
 
 
-def test_wave_sources_follow_wave_systems():
+def test_wave_sources_follow_wave_systems(csem_lib):
     import bench
     from demo_matrixfree_csem_gb300 import synthetic
     cfg = synthetic.workload("marlim_like_96")
     freqs = [float(f) for f in cfg.params["freqs"].split(",")]
     systems = [(f, s) for f in freqs for s in range(len(cfg.acq.src))]
+    mine = bench.rank_systems(systems, 2, 1, 11064870)
     for k in range(3):
-        f, src = bench.wave_systems(cfg, systems, 48, k, 0)
-        idx = bench.wave_sources(systems, 48, k)
-        assert np.array_equal(src, cfg.acq.src[idx, :3])
+        f, src = bench.wave_systems(cfg, mine, 48, k)
+        idx = bench.wave_sources(mine, 48, k)
+        want = cfg.acq.src[[i for i, _ in idx], :3].copy()
+        want[:, 1] += 50.0 * np.array([r for _, r in idx], np.float32)
+        assert np.array_equal(src, want)

@@ -1,5 +1,6 @@
-"""The multi-rank bench path on CPU: two gloo ranks partition the systems (disjoint
-sources, no exchange of solver data) and agree on the max-over-ranks timing."""
+"""The multi-rank bench path on CPU: two gloo ranks split the replicated system list with
+the product's partitioner (csem_partition_systems; disjoint units, equal expected work,
+no exchange of solver data) and agree on the max-over-ranks timing."""
 import os
 import socket
 import sys
@@ -30,9 +31,10 @@ def _worker(rank, world, port, out):
     cfg.acq.src = np.repeat(cfg.acq.src, 3, axis=0)
     cfg.acq.src[:, 0] += 100.0 * np.arange(3)
     systems = [(f, s) for f in (0.5, 1.0) for s in range(3)]
-    waves = [bench.wave_systems(cfg, systems, 4, k, rank) for k in range(2)]
+    mine = bench.rank_systems(systems, world, rank, 1000)
+    waves = [bench.wave_systems(cfg, mine, 4, k) for k in range(2)]
     wall = bench.max_over_ranks([1.0 + rank, 5.0 - rank], "cpu")
-    out[rank] = (waves, wall)
+    out[rank] = (waves, wall, mine)
     tdist.barrier()
     tdist.destroy_process_group()
 
@@ -49,9 +51,11 @@ def test_two_gloo_ranks_partition_and_reduce():
             p.join(120)
             assert p.exitcode == 0
         res = dict(out)
-    (w0, t0), (w1, t1) = res[0], res[1]
+    (w0, t0, m0), (w1, t1, m1) = res[0], res[1]
     assert t0 == t1 == [2.0, 5.0]                        # max over ranks, seen by every rank
+    assert not set(m0) & set(m1)                         # disjoint units
+    assert len(set(m0) | set(m1)) == 12                  # together: both copies of the 6 systems
+    assert sorted(f for f, _, _ in m0) == sorted(f for f, _, _ in m1)  # the same work on each rank
     for (f0, s0), (f1, s1) in zip(w0, w1):
-        assert np.array_equal(f0, f1)                    # same frequencies per step
-        assert not np.any(np.all(s0[:, None] == s1[None], axis=2))  # disjoint sources
+        assert not np.any(np.all(s0[:, None] == s1[None], axis=2))  # disjoint source positions
     assert [len(f) for f, _ in w0] == [4, 2]             # 6 systems in waves of 4
