@@ -67,7 +67,7 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK);  // the sweep's row
 // most rows_per_warp (4, 8, 16), vw march positions per step for Ey/Ez (1, 2, 4)
 void launch_sweep_tiled(const SweepP<F32>& s, int comp, bool fwd, int nslot, cudaStream_t st, int rows_per_warp,
                         int vw);
-bool sweep_tiled_fits(int comp, int n1, int n2, int nK, int rows_per_warp);  // at most 32 warps
+bool sweep_tiled_fits(int comp, int n1, int n2, int nK, int rows_per_warp, int vw);  // the rows fit one CTA
 template <class P>
 void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int nslot, cudaStream_t st);
 int sweep_diagonals(int comp, int n1, int n2, int nK);  // number of diagonals t (2..)

@@ -348,7 +348,7 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
   // dependency of the lexicographic sweep, so they may be mixed sweep by sweep
   auto sweep = [&](int comp, bool fwd) {
     if constexpr (!P::exact) {
-      if (tiled_sweeps && sweep_tiled_fits(comp, n1, n2, s.nK, tile_rows)) {
+      if (tiled_sweeps && sweep_tiled_fits(comp, n1, n2, s.nK, tile_rows, tile_vw)) {
         launch_sweep_tiled(s, comp, fwd, nslot, st, tile_rows, tile_vw);
         return;
       }
