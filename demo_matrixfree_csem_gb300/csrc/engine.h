@@ -57,11 +57,13 @@ template <class P> struct SweepP {
   const typename P::R *s11u, *s22u, *s33u;  // unshifted full-grid sigma (the Q2 lookups)
   const typename P::C* BV;  // divergence right-hand side [slot][lv]
   long lv;
+  int aphi_fix;             // 1: node sweeps with the conductivity-weighted diagonal (not the reference's)
 };
 
 // one launch per component sweep (pipelined warps, k_lusgs2.cu)
 template <class P>
-void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw);
+void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw,
+                            int prefetch = 1);
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK);  // the sweep's rows fit one CTA
 // complex64 line-tiled sweeps (k_lusgs3.cu): 32 lines per CTA, rows in warp blocks of at
 // most rows_per_warp (4, 8, 16), vw march positions per step for Ey/Ez (1, 2, 4)

@@ -354,7 +354,7 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
       }
     }
     if (pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
-      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st, sweep_vw);
+      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st, sweep_vw, sweep_prefetch);
       return;
     }
     const int nd = sweep_diagonals(comp, n1, n2, s.nK);
@@ -391,6 +391,7 @@ void Ops<P>::apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const 
   s.s11u = gu.s11;
   s.s22u = gu.s22;
   s.s33u = gu.s33;
+  s.aphi_fix = aphi_fix ? 1 : 0;
   const int n1 = m->n1, n2 = m->n2, n3 = m->n3;
   zero(Y, m->lE, nslot, sys_list);
   launch_aphi_div<P>(s, BV.as<C>(), nslot, st);

@@ -88,9 +88,13 @@ class Ops {
   // false = one launch per wavefront diagonal (k_lusgs.cu); both give identical results
   bool pipelined_sweeps = true;
   int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
+  int sweep_prefetch = 1;  // complex64: march positions the pipelined sweeps load ahead (1..3)
   // complex64 only: line-tiled sweeps (k_lusgs3.cu) instead of the pipelined ones, with
   // at most tile_rows rows per warp and tile_vw march positions per step (Ey, Ez)
   bool tiled_sweeps = false;
+  // A-phi node sweeps with the conductivity-weighted diagonal and consistently shifted
+  // conductivities instead of the reference's (an option; off reproduces the reference)
+  bool aphi_fix = false;
   int tile_rows = 8;
   int tile_vw = 4;
   // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal)

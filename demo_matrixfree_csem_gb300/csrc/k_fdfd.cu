@@ -246,7 +246,15 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
   const int gx = (g.n1 + 1 + 30) / 31, gy = (g.n2 + 1 + BY - 1) / BY;
   const long base = (long)gx * gy * nsys;
   // split the planes into chunks until about four CTAs per SM are in the grid
-  int nkc = (int)((4L * 152 + base - 1) / base);
+  static int sms[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    sms[dev] = 152;
+  }
+  int nkc = (int)((4L * sms[dev] + base - 1) / base);
   const int maxc = (g.n3 + 1) / 8 > 0 ? (g.n3 + 1) / 8 : 1;  // chunks of at least 8 planes
   if (nkc > maxc) nkc = maxc;
   if (nkc < 1) nkc = 1;

@@ -294,18 +294,32 @@ __global__ void k_aphi_phi(SweepP<P> s, typename P::C* __restrict__ VV, int t)
   const C vjp = FWD ? z : v[ixv(n1, n2, k, j + 1, i)], vjm = v[ixv(n1, n2, k, j - 1, i)];
   const C vkp = FWD ? z : v[ixv(n1, n2, k + 1, j, i)], vkm = v[ixv(n1, n2, k - 1, j, i)];
   const int kf = k + g.kstart;
-  C t1 = rmul<P>(g.s11[ix1(n1, n2, k, j, i)], cadd<P>(ax[ix1(n1, n2, k, j, i)], cdivs<P>(csub<P>(vip, vp), g.d1s[i], g.r1s[i])));
-  C t2 = rmul<P>(s.s11u[ix1(n1, n2, k, j, i - 1)], cadd<P>(ax[ix1(n1, n2, k, j, i - 1)], cdivs<P>(csub<P>(vp, vim), g.d1s[i - 1], g.r1s[i - 1])));
-  C t3 = rmul<P>(g.s22[ix2(n1, n2, k, j, i)], cadd<P>(ay[ix2(n1, n2, k, j, i)], cdivs<P>(csub<P>(vjp, vp), g.d2s[j], g.r2s[j])));
-  C t4 = rmul<P>(s.s22u[ix2(n1, n2, k, j - 1, i)], cadd<P>(ay[ix2(n1, n2, k, j - 1, i)], cdivs<P>(csub<P>(vp, vjm), g.d2s[j - 1], g.r2s[j - 1])));
-  C t5 = rmul<P>(g.s33[ix3(n1, n2, k, j, i)], cadd<P>(az[ix3(n1, n2, k, j, i)], cdivs<P>(csub<P>(vkp, vp), g.d3s[k], g.r3s[k])));
-  C t6 = rmul<P>(s.s33u[ix3(n1, n2, k - 1, j, i)], cadd<P>(az[ix3(n1, n2, k - 1, j, i)], cdivs<P>(csub<P>(vp, vkm), g.d3s[k - 1], g.r3s[k - 1])));
+  // the conductivities of the six faces around node (k,j,i): the reference reads the
+  // lower faces unshifted (Q2, fdfd.c:666,668,670,695,697,699); with aphi_fix all six
+  // come from the shifted operator-grid arrays
+  const R s1p = g.s11[ix1(n1, n2, k, j, i)], s2p = g.s22[ix2(n1, n2, k, j, i)], s3p = g.s33[ix3(n1, n2, k, j, i)];
+  const R s1m = s.aphi_fix ? g.s11[ix1(n1, n2, k, j, i - 1)] : s.s11u[ix1(n1, n2, k, j, i - 1)];
+  const R s2m = s.aphi_fix ? g.s22[ix2(n1, n2, k, j - 1, i)] : s.s22u[ix2(n1, n2, k, j - 1, i)];
+  const R s3m = s.aphi_fix ? g.s33[ix3(n1, n2, k - 1, j, i)] : s.s33u[ix3(n1, n2, k - 1, j, i)];
+  C t1 = rmul<P>(s1p, cadd<P>(ax[ix1(n1, n2, k, j, i)], cdivs<P>(csub<P>(vip, vp), g.d1s[i], g.r1s[i])));
+  C t2 = rmul<P>(s1m, cadd<P>(ax[ix1(n1, n2, k, j, i - 1)], cdivs<P>(csub<P>(vp, vim), g.d1s[i - 1], g.r1s[i - 1])));
+  C t3 = rmul<P>(s2p, cadd<P>(ay[ix2(n1, n2, k, j, i)], cdivs<P>(csub<P>(vjp, vp), g.d2s[j], g.r2s[j])));
+  C t4 = rmul<P>(s2m, cadd<P>(ay[ix2(n1, n2, k, j - 1, i)], cdivs<P>(csub<P>(vp, vjm), g.d2s[j - 1], g.r2s[j - 1])));
+  C t5 = rmul<P>(s3p, cadd<P>(az[ix3(n1, n2, k, j, i)], cdivs<P>(csub<P>(vkp, vp), g.d3s[k], g.r3s[k])));
+  C t6 = rmul<P>(s3m, cadd<P>(az[ix3(n1, n2, k - 1, j, i)], cdivs<P>(csub<P>(vp, vkm), g.d3s[k - 1], g.r3s[k - 1])));
   C aij = cadd<P>(cadd<P>(cdivs<P>(csub<P>(t1, t2), g.d1[i], g.r1[i]), cdivs<P>(csub<P>(t3, t4), g.d2[j], g.r2[j])),
                   cdivs<P>(csub<P>(t5, t6), g.d3[k], g.r3[k]));
   const R one = 1;
-  R geo = P::add(P::add(P::div(P::add(P::div(one, g.d1s[i]), P::div(one, g.d1s[i - 1])), g.d1[i]),
-                        P::div(P::add(P::div(one, g.d2s[j]), P::div(one, g.d2s[j - 1])), g.d2[j])),
-                 P::div(P::add(P::div(one, g.d3s[k]), P::div(one, g.d3s[k - 1])), g.d3[k]));
+  // the reference's diagonal is the plain Laplacian's (Q3, fdfd.c:672,701) although the
+  // couplings carry the face conductivities; with aphi_fix the diagonal carries them too,
+  // the diagonal of div(sigma grad v), so the node sweep is a Gauss-Seidel sweep of
+  // that operator
+  const R w1p = s.aphi_fix ? s1p : one, w1m = s.aphi_fix ? s1m : one;
+  const R w2p = s.aphi_fix ? s2p : one, w2m = s.aphi_fix ? s2m : one;
+  const R w3p = s.aphi_fix ? s3p : one, w3m = s.aphi_fix ? s3m : one;
+  R geo = P::add(P::add(P::div(P::add(P::div(w1p, g.d1s[i]), P::div(w1m, g.d1s[i - 1])), g.d1[i]),
+                        P::div(P::add(P::div(w2p, g.d2s[j]), P::div(w2m, g.d2s[j - 1])), g.d2[j])),
+                 P::div(P::add(P::div(w3p, g.d3s[k]), P::div(w3m, g.d3s[k - 1])), g.d3[k]));
   C aii = P::mk(-geo, 0);
   if (g.fvm) {
     C f = rmul<P>(P::mul(P::mul(g.d1s[i], g.d2[j]), g.d3[k]), sc.iom);

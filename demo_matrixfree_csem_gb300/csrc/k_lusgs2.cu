@@ -527,7 +527,7 @@ template <int VW> struct RawEyz {
 }  // namespace
 
 // Ex, complex64: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
-template <bool FWD, int VW, int MAXR>
+template <bool FWD, int VW, int MAXR, int PD>
 __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
 {
   typedef float2 C;
@@ -564,10 +564,12 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
   }
   const int L1 = n1 + 1;
   const float gn = Z.r * (FWD ? Z.rsm : Z.rs);
-  RawEx<VW> raw;
+  // operands of the next PD march positions: ring[q] holds position c+1+q at step
+  // T = c + rr (loads issued PD steps ahead of their use)
+  RawEx<VW> ring[PD];
   Lin32 lin[VW];
   // loads of march position c (nothing read here is written before that step)
-  auto load = [&](int c) {
+  auto load = [&](int c, RawEx<VW>& raw) {
     const int j = FWD ? 1 + c : M - c;
     raw.Y = axis<F32>(g.d2, g.d2s, g.r2, g.r2s, j);
     const int ox = j * n1, oy = j * L1;
@@ -591,7 +593,7 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
       }
     }
   };
-  auto make = [&]() {
+  auto make = [&](const RawEx<VW>& raw) {
     const Ax<F32>& Y = raw.Y;
     const float gg = (Y.rs + Y.rsm) * Y.r + (Z.rs + Z.rsm) * Z.r;  // geo(Y, Z)
     const float gp = Y.r * (FWD ? Y.rsm : Y.rs);
@@ -614,14 +616,20 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
   if (rowok && rr == 0 && M > 0) {
-    load(0);
-    make();
+    RawEx<VW> r0;
+    load(0, r0);
+    make(r0);
+  }
+#pragma unroll
+  for (int q = 0; q + 1 < PD; q++) {
+    const int p = 1 - rr + q;
+    if (rowok && p >= 0 && p < M) load(p, ring[q]);
   }
   for (int T = 0; T < M + R_ - 1; T++) {
     const int c = T - rr;
     const bool act = rowok && c >= 0 && c < M;
     const bool nxt = rowok && c + 1 >= 0 && c + 1 < M;
-    if (nxt) load(c + 1);
+    if (rowok && c + PD >= 0 && c + PD < M) load(c + PD, ring[PD - 1]);
     C nb[VW];
     hand.get(res, nb, T);
     if (act) {
@@ -641,14 +649,16 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
       for (int q = 0; q < VW; q++) res[q] = z;
     }
     hand.put(res, T);
-    if (nxt) make();
+    if (nxt) make(ring[0]);
+#pragma unroll
+    for (int q = 0; q + 1 < PD; q++) ring[q] = ring[q + 1];
   }
   hand.finish(M + R_ - 1);
 }
 
 // Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j), complex64: march i in
 // chunks of VW. grid (lines, systems)
-template <int COMP, bool FWD, int VW, int MAXR>
+template <int COMP, bool FWD, int VW, int MAXR, int PD>
 __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
 {
   typedef float2 C;
@@ -710,9 +720,9 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
   const float gn = Rw.r * (FWD ? Rw.rsm : Rw.rs);
   // the coefficient of the line-axis differences in cross: Y.rs (Ey) or Z.rs (Ez)
   const float lrs = COMP == 1 ? Y.rs : Z.rs;
-  RawEyz<VW> raw;
+  RawEyz<VW> ring[PD];  // ring[q]: operands of position c+1+q at step T = c + rr
   Lin32 lin[VW];
-  auto load = [&](int c) {
+  auto load = [&](int c, RawEyz<VW>& raw) {
 #pragma unroll
     for (int q = 0; q < VW; q++) {
       const int m = c * VW + q;
@@ -738,7 +748,7 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
       }
     }
   };
-  auto make = [&](int c) {
+  auto make = [&](int c, const RawEyz<VW>& raw) {
 #pragma unroll
     for (int q = 0; q < VW; q++) {
       if (c * VW + q >= M) continue;
@@ -764,14 +774,20 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
   if (rowok && rr == 0 && NC > 0) {
-    load(0);
-    make(0);
+    RawEyz<VW> r0;
+    load(0, r0);
+    make(0, r0);
+  }
+#pragma unroll
+  for (int q = 0; q + 1 < PD; q++) {
+    const int p = 1 - rr + q;
+    if (rowok && p >= 0 && p < NC) load(p, ring[q]);
   }
   for (int T = 0; T < NC + R_ - 1; T++) {
     const int c = T - rr;
     const bool act = rowok && c >= 0 && c < NC;
     const bool nx = rowok && c + 1 >= 0 && c + 1 < NC;
-    if (nx) load(c + 1);
+    if (rowok && c + PD >= 0 && c + PD < NC) load(c + PD, ring[PD - 1]);
     C nb[VW];
     hand.get(res, nb, T);
     if (act) {
@@ -793,7 +809,9 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
       for (int q = 0; q < VW; q++) res[q] = z;
     }
     hand.put(res, T);
-    if (nx) make(c + 1);
+    if (nx) make(c + 1, ring[0]);
+#pragma unroll
+    for (int q = 0; q + 1 < PD; q++) ring[q] = ring[q + 1];
   }
   hand.finish(NC + R_ - 1);
 }
@@ -804,7 +822,7 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
   return rows >= 1 && rows <= MAXROWS && n1 >= 2 && n2 >= 2;
 }
 
-template <class P, int VW, int MAXR>
+template <class P, int VW, int MAXR, int PD>
 static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st)
 {
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
@@ -813,16 +831,16 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
   if constexpr (!P::exact) {  // complex64: the linear-form sweeps
     if (comp == 0) {
       dim3 grd((n1 + VW - 1) / VW, nslot);
-      if (fwd) count_launch(), k_sweep_ex32<true, VW, MAXR><<<grd, threads, 0, st>>>(s);
-      else count_launch(), k_sweep_ex32<false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      if (fwd) count_launch(), k_sweep_ex32<true, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_ex32<false, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
     } else if (comp == 1) {
       dim3 grd(n2, nslot);
-      if (fwd) count_launch(), k_sweep_eyz32<1, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
-      else count_launch(), k_sweep_eyz32<1, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      if (fwd) count_launch(), k_sweep_eyz32<1, true, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_eyz32<1, false, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
     } else {
       dim3 grd(nK, nslot);
-      if (fwd) count_launch(), k_sweep_eyz32<2, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
-      else count_launch(), k_sweep_eyz32<2, false, VW, MAXR><<<grd, threads, 0, st>>>(s);
+      if (fwd) count_launch(), k_sweep_eyz32<2, true, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
+      else count_launch(), k_sweep_eyz32<2, false, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
     }
   } else {  // complex128: the reference's operation order
     if (comp == 0) {
@@ -844,22 +862,33 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
 // vw: points per thread and step (1, 2 or 4; other values select the default, the
 // fastest measured on a 200x140x140 grid: 2 for complex64, 1 for complex128). Sweeps of
 // more than 256 rows run 1 or 2 points per thread in CTAs of up to 512 threads.
-template <class P>
-void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw)
+template <class P, int PD>
+static void launch_pd(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw)
 {
-  if (vw != 1 && vw != 2 && vw != 4) vw = P::exact ? 1 : 2;
   const int rows = comp == 2 ? s.g.n2 - 1 : s.nK - 1;
   if (rows > NB_ROWS) {
-    if (vw == 1) launch_vw<P, 1, MAXROWS>(s, comp, fwd, nslot, st);
-    else launch_vw<P, 2, MAXROWS>(s, comp, fwd, nslot, st);
+    if (vw == 1) launch_vw<P, 1, MAXROWS, PD>(s, comp, fwd, nslot, st);
+    else launch_vw<P, 2, MAXROWS, PD>(s, comp, fwd, nslot, st);
     return;
   }
-  if (vw == 1) launch_vw<P, 1, NB_ROWS>(s, comp, fwd, nslot, st);
-  else if (vw == 2) launch_vw<P, 2, NB_ROWS>(s, comp, fwd, nslot, st);
-  else launch_vw<P, 4, NB_ROWS>(s, comp, fwd, nslot, st);
+  if (vw == 1) launch_vw<P, 1, NB_ROWS, PD>(s, comp, fwd, nslot, st);
+  else if (vw == 2) launch_vw<P, 2, NB_ROWS, PD>(s, comp, fwd, nslot, st);
+  else launch_vw<P, 4, NB_ROWS, PD>(s, comp, fwd, nslot, st);
 }
 
-template void launch_sweep_pipelined<F64>(const SweepP<F64>&, int, bool, int, cudaStream_t, int);
-template void launch_sweep_pipelined<F32>(const SweepP<F32>&, int, bool, int, cudaStream_t, int);
+// prefetch: march positions the complex64 sweeps load ahead of use (1, 2 or 3; the
+// complex128 sweeps always load one position ahead)
+template <class P>
+void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw,
+                            int prefetch)
+{
+  if (vw != 1 && vw != 2 && vw != 4) vw = P::exact ? 1 : 2;
+  if (P::exact || prefetch <= 1) launch_pd<P, 1>(s, comp, fwd, nslot, st, vw);
+  else if (prefetch == 2) launch_pd<P, 2>(s, comp, fwd, nslot, st, vw);
+  else launch_pd<P, 3>(s, comp, fwd, nslot, st, vw);
+}
+
+template void launch_sweep_pipelined<F64>(const SweepP<F64>&, int, bool, int, cudaStream_t, int, int);
+template void launch_sweep_pipelined<F32>(const SweepP<F32>&, int, bool, int, cudaStream_t, int, int);
 
 }  // namespace csem

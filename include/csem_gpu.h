@@ -231,6 +231,14 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     (one lane each), the rows cut into one block per warp; 0: the
  *                     schedule chosen by lusgs_pipelined. Same values as the pipelined
  *                     complex64 sweeps;
+ *   "aphi_fix"        1: the A-phi preconditioner's node-potential sweeps use the
+ *                     diagonal of div(sigma grad v), the face conductivities on it as on
+ *                     the couplings, all read from the operator grid; 0 (default): the
+ *                     reference's sweeps (fdfd.c:655-710), whose diagonal omits the
+ *                     conductivities and whose lower-face lookups skip the air-layer shift,
+ *                     so a sweep through seawater (sigma > 1 S/m) amplifies its input
+ *                     geometrically (about 1e44 for a unit input on a 125 x 125 x 100 cell
+ *                     bathymetry model). This option changes results;
  *   "lusgs_tile_rows" rows per warp block of the tiled sweeps: 4, 8 (default) or 16;
  *   "lusgs_tile_vw"   march positions per step of the tiled Ey and Ez sweeps: 1, 2 or 4
  *                     (default);

@@ -1,0 +1,92 @@
+"""The A-phi preconditioner with the conductivity-weighted node diagonal (aphi_fix).
+
+The reference's node-potential sweeps (fdfd.c:655-710) divide by the diagonal of the plain
+Laplacian while their couplings carry the face conductivities, and read the lower faces'
+conductivities without the air-layer shift. Through seawater (sigma = 3.3 S/m) each node
+update then multiplies the error of the previous one, and a sweep amplifies a unit
+input geometrically: about 1e44 on the bathymetry model, beyond the complex64 range, so
+the mixed-precision path cannot use it (tests/test_gpu_uneven.py). With aphi_fix the
+diagonal is that of div(sigma grad v) and every conductivity comes from the operator
+grid, so the node sweep is an ordinary Gauss-Seidel sweep.
+
+Checked here: the option leaves the reference's behaviour untouched when off; with it
+the preconditioner stays bounded on the bathymetry model; and complex64 GMRES(10) with
+the fixed A-phi inside complex128 defect correction converges to the receivers the
+complex128 BiCGStab + LU-SGS solver gives, to 1e-6 (both stop at tol = 1e-8/f on the
+true residual)."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import demo_matrixfree_csem_gb300 as cs
+from cases import oracle_for, probe, product_grid, relerr
+from demo_matrixfree_csem_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def test_option_off_keeps_reference_aphi(gpu, tmp_path):
+    cfg = synthetic.random_small(81, nx=20, ny=17, nz=12, nb=3, airbc=1, n1fft=32, n2fft=32, preco=3)
+    synthetic.write_config(cfg, str(tmp_path))
+    p = {k: str(v) for k, v in cfg.params.items()}
+    G = product_grid(str(tmp_path), p)
+    ctx = cs.Ctx(G, 1, 0)
+    O = oracle_for(G, p)
+    O.set_freq(0.75)
+    x = probe(ctx.lE, 4)
+    ref = O.aphi(x)
+    ctx.set_option("aphi_fix", 1)
+    fixed = ctx.aphi_apply(cs.iom_of(0.75), x)
+    ctx.set_option("aphi_fix", 0)
+    assert np.array_equal(ctx.aphi_apply(cs.iom_of(0.75), x), ref)
+    assert not np.array_equal(fixed, ref)
+
+
+def test_fixed_aphi_is_bounded_on_bathymetry(gpu):
+    cfg = synthetic.bathymetry_125()
+    cfg.params["nb"] = 8
+    with tempfile.TemporaryDirectory() as d:
+        G = synthetic.build_grid(cfg, d)
+    ctx = cs.Ctx(G, 1, 0)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(ctx.lE) + 1j * rng.standard_normal(ctx.lE)
+    iom = cs.iom_of(0.25)
+    y_ref = ctx.aphi_apply(iom, x)
+    y_lu = ctx.lusgs_apply(iom, x)
+    ctx.set_option("aphi_fix", 1)
+    y_fix = ctx.aphi_apply(iom, x)
+    y_fix32 = ctx.aphi_apply(iom, x.astype(np.complex64), c64=True)
+    print(f"max |M^-1 x|: reference A-phi {np.abs(y_ref).max():.3e}, fixed A-phi {np.abs(y_fix).max():.3e}, "
+          f"LU-SGS {np.abs(y_lu).max():.3e}; complex64 fixed vs complex128 fixed {relerr(y_fix32, y_fix):.2e}")
+    assert np.abs(y_ref).max() > 1e38
+    assert np.all(np.isfinite(y_fix)) and np.abs(y_fix).max() < 1e6 * max(np.abs(y_lu).max(), 1.0)
+    assert relerr(y_fix32, y_fix) <= 1e-4
+
+
+@pytest.mark.parametrize("model", ["random", "bathymetry"])
+def test_mixed_gmres_with_fixed_aphi_converges(gpu, tmp_path, model):
+    if model == "random":
+        cfg = synthetic.random_small(82, nx=24, ny=20, nz=14, nb=4, airbc=1, n1fft=64, n2fft=64)
+        synthetic.write_config(cfg, str(tmp_path))
+        G = product_grid(str(tmp_path), {k: str(v) for k, v in cfg.params.items()})
+        freqs = np.array([0.5, 1.0], np.float32)
+    else:
+        cfg = synthetic.bathymetry_125()
+        cfg.params["nb"] = 10
+        with tempfile.TemporaryDirectory() as d:
+            G = synthetic.build_grid(cfg, d)
+        freqs = np.array([1.25, 1.25], np.float32)
+    ctx = cs.Ctx(G, 1, 0)
+    src = np.repeat(cfg.acq.src[:1, :3], 2, axis=0)
+    src[1, 0] += 300.0 if model == "bathymetry" else 30.0
+    ref = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=64, algopt=1, preco=1, niter=3000, tol=1e-8)
+    assert ref["status"] == ["converged"] * 2
+    ctx.set_option("aphi_fix", 1)
+    got = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=32, algopt=2, nrestart=10, preco=3, niter=3000,
+                         tol=1e-8, max_outer=60)
+    print(f"{model}: GMRES(10) + fixed A-phi: status {got['status']}, inner iterations {got['iters'].tolist()}, "
+          f"defect corrections {got['outer'].tolist()}; complex128 BiCGStab + LU-SGS iterations {ref['iters'].tolist()}")
+    assert got["status"] == ["converged"] * 2
+    for q in range(2):
+        assert relerr(got["dcal"][q], ref["dcal"][q]) <= 1e-6, relerr(got["dcal"][q], ref["dcal"][q])

@@ -36,7 +36,7 @@ def test_driver_writes_reference_files(gpu, case, tmp_path):
     from demo_matrixfree_csem_gb300 import build
     d, args, gold = load_golden(case)
     for f in os.listdir(d):
-        if f not in ("golden.npz", "args.json"):
+        if os.path.isfile(os.path.join(d, f)) and f not in ("golden.npz", "args.json"):
             shutil.copy(os.path.join(d, f), tmp_path / f)
     p = parse_args(args)
     f0 = float(gold["freqs"][0])
@@ -56,3 +56,69 @@ def test_driver_writes_reference_files(gpu, case, tmp_path):
     printed = gold["hist_printed"]
     assert len(hist) == len(printed) + 1
     assert [float(ln.split()[1]) for ln in hist[1:]] == [float("%e" % v) for v in printed]
+
+
+def test_driver_all_sources_writes_one_file_per_source(gpu, tmp_path):
+    """nsrc=all solves every source row (the reference solves only the first,
+    acq_init_free.c:56,90) and writes emf_0001.txt, emf_0002.txt, ... in the
+    write_data.c:24-32 format, source s with iTx = s. Each file equals what the driver
+    writes for that source alone (iTx aside), and the batched mixed-precision driver
+    (precision=32) gives the same receivers to complex64 output precision."""
+    from demo_matrixfree_csem_gb300 import build
+    case = "lusgs_air0"
+    d, args, gold = load_golden(case)
+    for f in os.listdir(d):
+        if os.path.isfile(os.path.join(d, f)) and f not in ("golden.npz", "args.json", "acsr.npz"):
+            shutil.copy(os.path.join(d, f), tmp_path / f)
+    lines = open(tmp_path / "sources.txt").read().splitlines()
+    head, row = lines[0], lines[1].split()
+    srcs = []
+    for s, dx in enumerate((0.0, 45.0, -60.0)):
+        r = list(row)
+        r[0] = "%f" % (float(row[0]) + dx)
+        r[5] = str(s + 1)
+        srcs.append(" ".join(r))
+        (tmp_path / f"one_{s + 1}.txt").write_text(head + "\n" + " ".join(r[:5] + ["1"]) + "\n")
+    (tmp_path / "three.txt").write_text(head + "\n" + "\n".join(srcs) + "\n")
+    base = [a for a in args[1:] if not a.startswith("fsrc=")] + ["niter=400"]
+
+    def run(extra, cwd):
+        r = subprocess.run([build.DRIVER, *base, *extra], cwd=cwd, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        return r
+
+    all_dir = tmp_path / "all"
+    all_dir.mkdir()
+    for f in os.listdir(tmp_path):
+        if os.path.isfile(tmp_path / f):
+            shutil.copy(tmp_path / f, all_dir / f)
+    run(["fsrc=three.txt", "nsrc=all"], all_dir)
+    p = parse_args(args)
+    nfreq, nch = len(p["freqs"].split(",")), len(p["chrec"].split(","))
+    for s in range(3):
+        one = tmp_path / f"single_{s + 1}"
+        one.mkdir()
+        for f in os.listdir(tmp_path):
+            if os.path.isfile(tmp_path / f):
+                shutil.copy(tmp_path / f, one / f)
+        run([f"fsrc=one_{s + 1}.txt"], one)
+        got = open(all_dir / f"emf_{s + 1:04d}.txt").read().splitlines()
+        want = open(one / "emf_0001.txt").read().splitlines()
+        assert got[0] == want[0] == "iTx \t iRx    ichrec  ifreq \t emf_real \t emf_imag"
+        assert len(got) == 1 + nch * nfreq * len(gold["dcal"][0])
+        for g_, w_ in zip(got[1:], want[1:]):
+            gf, wf = g_.split(" \t "), w_.split(" \t ")
+            assert gf[0] == str(s + 1) and wf[0] == "1" and gf[1:] == wf[1:]
+    assert not os.path.exists(all_dir / "emf_0004.txt")
+    mixed = tmp_path / "mixed"
+    mixed.mkdir()
+    for f in os.listdir(tmp_path):
+        if os.path.isfile(tmp_path / f):
+            shutil.copy(tmp_path / f, mixed / f)
+    run(["fsrc=three.txt", "nsrc=all", "precision=32"], mixed)
+    for s in range(3):
+        a = np.array([[float(v) for v in ln.split(" \t ")[4:6]] for ln in
+                      open(all_dir / f"emf_{s + 1:04d}.txt").read().splitlines()[1:]])
+        b = np.array([[float(v) for v in ln.split(" \t ")[4:6]] for ln in
+                      open(mixed / f"emf_{s + 1:04d}.txt").read().splitlines()[1:]])
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
