@@ -16,6 +16,7 @@
 #include <complex>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include "solve_mixed.h"
 #include "../../include/csem_gpu.h"
 
@@ -71,10 +72,18 @@ MixedBatch::MixedBatch(Model* m_, int nsys_, cudaStream_t st_)
   rn.alloc(sizeof(double) * nsys);
 }
 
+void MixedBatch::drop_gmres_graphs()
+{
+  for (auto& kv : gm_graphs_)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  gm_graphs_.clear();
+}
+
 MixedBatch::~MixedBatch()
 {
-  for (auto& kv : graphs_)
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  for (auto* m : {&graphs_, &gm_graphs_})
+    for (auto& kv : *m)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
 }
 
 // The iterations between two status reads are the same launch sequence every time for a
@@ -83,19 +92,10 @@ MixedBatch::~MixedBatch()
 // graph. The first occurrence runs directly, which also creates everything created on
 // first use (FFT plans, A-phi work arrays) before any capture. Per-operator profiling
 // records events per application, so it keeps the direct launches.
-void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
+void MixedBatch::run_captured(Graph& g, bool use_graphs, const std::function<void()>& body)
 {
-  const int* dl = list.as<int>();
-  auto direct = [&]() {
-    for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
-  };
-  if (!o.graphs || prof_on()) {
-    direct();
-    return;
-  }
-  Graph& g = graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter)];
-  if (g.failed || g.seen++ == 0) {
-    direct();
+  if (!use_graphs || prof_on() || g.failed || g.seen++ == 0) {
+    body();
     return;
   }
   if (!g.exec) {
@@ -103,7 +103,7 @@ void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
     const long long l0 = csem_launch_count();
     CSEM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
+      body();
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -117,13 +117,21 @@ void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
       (void)cudaGetLastError();
       g.exec = nullptr;
       g.failed = true;
-      direct();
+      body();
       return;
     }
     cudaGraphDestroy(graph);
   }
   CSEM_CUDA_TRY(cudaGraphLaunch(g.exec, st));
   count_launch(g.launches);
+}
+
+void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
+{
+  const int* dl = list.as<int>();
+  run_captured(graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter)], o.graphs, [&]() {
+    for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
+  });
 }
 
 void MixedBatch::inject(const float* src, const double* iom, int nch, const int* ch)
@@ -334,26 +342,157 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
 // The same defect correction with a complex64 flexible GMRES(m) as the inner solver, the
 // structure of fgmres (solver.c:403-512): z_j = M v_j, w = A z_j, modified Gram-Schmidt
 // against v_0..v_j, Givens rotations of the Hessenberg column, restart after m steps.
-// Vectors, preconditioner, operator and dot products run batched on the device over the
-// systems still iterating; the (m+1) x m Hessenberg algebra of every system runs in
-// complex128 on the host (one read of the batched dot products per Gram-Schmidt step).
-// A system leaves the step loop of a cycle when its estimated residual reaches the inner
-// reduction.
+// Everything runs on the device over the systems of the cycle: the vectors, the
+// preconditioner, the operator and the dot products batched, and each system's
+// (m+1) x m Hessenberg algebra in complex128 by one thread per system (k_gm_*), reading
+// the dot products where the reduction left them. A system whose estimated residual
+// reaches the inner reduction stops stepping (its later steps are skipped by these
+// kernels and its update uses only the steps it took); the host reads the systems' state
+// once per cycle to choose the next cycle's systems. The m steps of a cycle are one
+// fixed launch sequence for a given number of systems, replayed as a CUDA graph from the
+// second time it occurs.
 namespace {
-typedef std::complex<double> zc;
-inline zc Z(double2 v) { return zc(v.x, v.y); }
-inline double2 D2(zc v) { return make_double2(v.real(), v.imag()); }
-}  // namespace
 
-std::vector<double2> MixedBatch::batch_dot(const float2* a, const float2* b, int ng, const int* dl)
+struct GmState {
+  double beta0;  // |r0| of the solve's first cycle: the residual estimates refer to it
+  double tol;    // relative reduction asked of this inner solve
+  int steps;     // Arnoldi steps taken in the current cycle
+  int iters;     // steps taken in this inner solve
+  int niter;     // step budget (the reference's niter)
+  int stop;      // 1: no more steps in this cycle
+  int done;      // 1: the reduction is reached (or the Krylov space is exhausted)
+  int pad;
+};
+
+__device__ __forceinline__ double2 zmul(double2 a, double2 b)
 {
-  double2* Dd = dots.as<double2>();
-  launch_dot<F32>(a, b, n, n, ng, dl, partial.as<double2>(), nblk, Dd, st);
-  std::vector<double2> h(ng);
-  CSEM_CUDA_TRY(cudaMemcpyAsync(h.data(), Dd, sizeof(double2) * ng, cudaMemcpyDeviceToHost, st));
-  CSEM_CUDA_TRY(cudaStreamSynchronize(st));
-  return h;
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 zscl(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+__device__ __forceinline__ double2 zdiv(double2 a, double2 b)  // Smith's quotient
+{
+  if (fabs(b.x) < fabs(b.y)) {
+    const double r = b.x / b.y, den = b.x * r + b.y;
+    return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+  }
+  const double r = b.y / b.x, den = b.y * r + b.x;
+  return make_double2((a.y * r + a.x) / den, (a.y - a.x * r) / den);
+}
+
+// cycle start: beta = |r| from its dot product, g = (beta, 0, ..), the divisor of v_0
+__global__ void k_gm_begin(int nact, const int* __restrict__ list, GmState* __restrict__ st,
+                           const double2* __restrict__ drr, double2* __restrict__ g, double2* __restrict__ coef, int m,
+                           int first)
+{
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= nact) return;
+  const int sys = list[slot];
+  GmState& S = st[sys];
+  const double beta = sqrt(drr[slot].x);
+  if (first) S.beta0 = beta > 0 ? beta : 1.0;
+  double2* gs = g + (size_t)sys * (m + 1);
+  gs[0] = make_double2(beta, 0.0);
+  for (int i = 1; i <= m; i++) gs[i] = make_double2(0.0, 0.0);
+  coef[slot] = make_double2(beta > 0 ? beta : 1.0, 0.0);
+  S.steps = 0;
+  S.stop = 0;
+}
+
+// step j: Hessenberg column j from the Gram-Schmidt dots (slot-indexed rows i = 0..j of
+// dots, the norm in row m), earlier rotations, the new rotation, the residual estimate
+// (as the host algebra of fgmres, solver.c:448-481) and the divisor of v_{j+1}
+__global__ void k_gm_step(int nact, const int* __restrict__ list, GmState* __restrict__ st,
+                          const double2* __restrict__ dots, int dstride, double2* __restrict__ H,
+                          double2* __restrict__ cs, double* __restrict__ sn, double2* __restrict__ g,
+                          double2* __restrict__ coef, int m, int j)
+{
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= nact) return;
+  const int sys = list[slot];
+  GmState& S = st[sys];
+  const double nn = dots[(size_t)m * dstride + slot].x;
+  const double hn = sqrt(nn);
+  coef[slot] = make_double2(hn > 0 ? hn : 1.0, 0.0);
+  if (S.stop) return;
+  double2* col = H + ((size_t)sys * m + j) * (m + 1);
+  double2* c = cs + (size_t)sys * m;
+  double* s = sn + (size_t)sys * m;
+  double2* gs = g + (size_t)sys * (m + 1);
+  for (int i = 0; i <= j; i++) col[i] = dots[(size_t)i * dstride + slot];
+  col[j + 1] = make_double2(hn, 0.0);
+  for (int i = 0; i < j; i++) {  // earlier rotations
+    const double2 t = zadd(zmul(zconj(c[i]), col[i]), zscl(s[i], col[i + 1]));
+    col[i + 1] = zadd(zscl(-s[i], col[i]), zmul(c[i], col[i + 1]));
+    col[i] = t;
+  }
+  const double tmp = sqrt((col[j].x * col[j].x + col[j].y * col[j].y) +
+                          (col[j + 1].x * col[j + 1].x + col[j + 1].y * col[j + 1].y));
+  if (tmp == 0.0) {
+    S.stop = 1;
+    return;
+  }
+  s[j] = col[j + 1].x / tmp;
+  c[j] = make_double2(col[j].x / tmp, col[j].y / tmp);
+  gs[j + 1] = zscl(-s[j], gs[j]);
+  gs[j] = zmul(zconj(c[j]), gs[j]);
+  col[j] = zadd(zmul(zconj(c[j]), col[j]), zscl(s[j], col[j + 1]));
+  S.steps = j + 1;
+  S.iters += 1;
+  const double rel = hypot(gs[j + 1].x, gs[j + 1].y) / S.beta0;
+  if (rel < S.tol || !(nn > 0.0)) {
+    S.stop = 1;
+    S.done = 1;
+  } else if (S.iters >= S.niter) {
+    S.stop = 1;
+  }
+}
+
+// y from the triangular system of the steps each system took (solver.c:489-495);
+// y[i][slot] = 0 past them
+__global__ void k_gm_solve(int nact, const int* __restrict__ list, const GmState* __restrict__ st,
+                           const double2* __restrict__ H, const double2* __restrict__ g, double2* __restrict__ y,
+                           int ystride, int m)
+{
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= nact) return;
+  const int sys = list[slot];
+  const int mm = st[sys].steps;
+  const double2* Hs = H + (size_t)sys * m * (m + 1);  // column k at Hs[k * (m + 1)]
+  const double2* gs = g + (size_t)sys * (m + 1);
+  double2 yv[64];
+  for (int i = mm - 1; i >= 0; i--) {
+    double2 acc = gs[i];
+    for (int k2 = i + 1; k2 < mm; k2++) acc = zsub(acc, zmul(Hs[(size_t)k2 * (m + 1) + i], yv[k2]));
+    yv[i] = zdiv(acc, Hs[(size_t)i * (m + 1) + i]);
+  }
+  for (int i = 0; i < m; i++) y[(size_t)i * ystride + slot] = i < mm ? yv[i] : make_double2(0.0, 0.0);
+}
+
+// d += sum_{i < steps} y_i z_i (solver.c:496-500), the systems' own step counts
+__global__ void k_gm_update(long n, const int* __restrict__ list, const GmState* __restrict__ st,
+                            const double2* __restrict__ y, int ystride, const float2* __restrict__ Z, size_t zstride,
+                            float2* __restrict__ d)
+{
+  const int slot = blockIdx.y;
+  const int sys = list[slot];
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const size_t o = (size_t)sys * n + q;
+  const int mm = st[sys].steps;
+  float2 acc = d[o];
+  for (int i = 0; i < mm; i++) {
+    const double2 a2 = y[(size_t)i * ystride + slot];
+    const float2 a = make_float2((float)a2.x, (float)a2.y);
+    const float2 z = Z[(size_t)i * zstride + o];
+    acc = make_float2(acc.x + (a.x * z.x - a.y * z.y), acc.y + (a.x * z.y + a.y * z.x));
+  }
+  d[o] = acc;
+}
+
+}  // namespace
 
 void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double>& tol_inner, const MixedOptions& o,
                              std::vector<int>& iters)
@@ -367,132 +506,88 @@ void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double
   float2* GD = base + (size_t)(2 * m + 2) * N;
   float2* GR0 = base + (size_t)(2 * m + 3) * N;
   const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
-  double2* cf = gcoef.as<double2>();
-  auto M = [&](const float2* in, float2* out, int ng, const int* dl) {  // Z_j: only written here
-    if (o.preco == PRE_APHI) o32.apply_aphi(in, out, ng, dl, sc);
-    else o32.apply_lusgs(in, out, ng, dl, sc, true);
+  // device state: GmState[nsys] | H [nsys][m][m+1] | cs [nsys][m] | g [nsys][m+1] |
+  // dots [m+2][nsys] | y [m][nsys] | coef [nsys] (double2), then sn [nsys][m] (double)
+  const size_t nst = ((sizeof(GmState) * nsys + 15) / 16) * 16;
+  const size_t nz = (size_t)nsys * ((size_t)m * (m + 1) + m + (m + 1) + (m + 2) + m + 1);
+  const size_t need = nst + sizeof(double2) * nz + sizeof(double) * (size_t)nsys * m;
+  if (gstate.bytes < need) {
+    drop_gmres_graphs();  // they hold the old buffer's addresses
+    gstate.alloc(need);
+  }
+  char* gb = gstate.as<char>();
+  GmState* st = reinterpret_cast<GmState*>(gb);
+  double2* zb = reinterpret_cast<double2*>(gb + nst);
+  double2* H = zb;
+  double2* cs = H + (size_t)nsys * m * (m + 1);
+  double2* gg = cs + (size_t)nsys * m;
+  double2* dots = gg + (size_t)nsys * (m + 1);
+  double2* ycoef = dots + (size_t)(m + 2) * nsys;
+  double2* coef = ycoef + (size_t)m * nsys;
+  double* sn = reinterpret_cast<double*>(coef + nsys);
+  const int ns = (int)g.size();
+  std::vector<GmState> sh(nsys);
+  memset(sh.data(), 0, sizeof(GmState) * nsys);
+  for (int q = 0; q < ns; q++) {
+    sh[g[q]].tol = tol_inner[q];
+    sh[g[q]].niter = o.niter;
+  }
+  CSEM_CUDA_TRY(cudaMemcpyAsync(st, sh.data(), sizeof(GmState) * nsys, cudaMemcpyHostToDevice, this->st));
+  auto M = [&](const float2* in, float2* out, int na, const int* dl) {  // Z_j: only written here
+    if (o.preco == PRE_APHI) o32.apply_aphi(in, out, na, dl, sc);
+    else o32.apply_lusgs(in, out, na, dl, sc, true);
   };
   // r0 = r64 / |r64|, d = 0 (k_start_inner writes r, r0, p, d: here r0 twice and d)
   {
-    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, g.data(), sizeof(int) * g.size(), cudaMemcpyHostToDevice, st));
+    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, g.data(), sizeof(int) * g.size(), cudaMemcpyHostToDevice, this->st));
     dim3 grd((unsigned)((n + 255) / 256), (unsigned)g.size());
-    count_launch(), k_start_inner<<<grd, 256, 0, st>>>(n, list.as<int>(), rn.as<double>(), r64.as<double2>(), GR0, GR0,
-                                                       GW, GD);
+    count_launch(), k_start_inner<<<grd, 256, 0, this->st>>>(n, list.as<int>(), rn.as<double>(), r64.as<double2>(),
+                                                             GR0, GR0, GW, GD);
   }
-  const int ns = (int)g.size();
-  std::vector<double> beta0(ns, 1.0);
-  std::vector<char> done(ns, 0);
-  iters.assign(ns, 0);
-  std::vector<int> lists(nsys);
+  const int* dl = list.as<int>();
   for (int cycle = 0;; cycle++) {
-    std::vector<int> act;  // positions in g of systems still solving
+    std::vector<int> act;
     for (int q = 0; q < ns; q++)
-      if (!done[q] && iters[q] < o.niter) act.push_back(q);
+      if (!sh[g[q]].done && sh[g[q]].iters < o.niter) act.push_back(g[q]);
     if (act.empty()) break;
-    int na = (int)act.size();
-    std::vector<int> sl(na);
-    for (int a = 0; a < na; a++) sl[a] = g[act[a]];
-    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, sl.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st));
-    const int* dl = list.as<int>();
-    // r = r0 - A d  (d = 0 on the first cycle)
+    const int na = (int)act.size();
+    const unsigned nb32 = (unsigned)((na + 31) / 32);
+    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, act.data(), sizeof(int) * na, cudaMemcpyHostToDevice, this->st));
+    // r = r0 - A d  (d = 0 on the first cycle), v_0 = r / |r|
     if (cycle == 0) {
-      CSEM_CUDA_TRY(cudaMemcpyAsync(GW, GR0, sizeof(float2) * N, cudaMemcpyDeviceToDevice, st));
+      CSEM_CUDA_TRY(cudaMemcpyAsync(GW, GR0, sizeof(float2) * N, cudaMemcpyDeviceToDevice, this->st));
     } else {
       o32.apply_A(GD, GV(0), na, dl, sc);
-      launch_vec<F32>(VEC_SUB, n, na, dl, nullptr, GR0, GV(0), GW, nullptr, nullptr, st);
+      launch_vec<F32>(VEC_SUB, n, na, dl, nullptr, GR0, GV(0), GW, nullptr, nullptr, this->st);
     }
-    std::vector<double2> bb = batch_dot(GW, GW, na, dl);
-    std::vector<double> beta(na);
-    std::vector<double2> cdiv(na);
-    for (int a = 0; a < na; a++) {
-      beta[a] = std::sqrt(bb[a].x);
-      if (cycle == 0) beta0[act[a]] = beta[a] > 0 ? beta[a] : 1.0;
-      cdiv[a] = make_double2(beta[a] > 0 ? beta[a] : 1.0, 0.0);
-    }
-    CSEM_CUDA_TRY(cudaMemcpyAsync(cf, cdiv.data(), sizeof(double2) * na, cudaMemcpyHostToDevice, st));
-    launch_cdivv<F32>(n, na, dl, cf, 1, 1, GW, GV(0), st);
-    // per-system Hessenberg (column j in H[j][0..j+1]), Givens and right-hand side
-    std::vector<std::vector<zc>> H(na, std::vector<zc>((size_t)m * (m + 1))), gg(na, std::vector<zc>(m + 1));
-    std::vector<std::vector<zc>> cs(na, std::vector<zc>(m));
-    std::vector<std::vector<double>> sn(na, std::vector<double>(m));
-    std::vector<int> steps(na, 0);
-    std::vector<char> stop(na, 0);
-    for (int a = 0; a < na; a++) gg[a][0] = zc(beta[a], 0.0);
-    for (int j = 0; j < m; j++) {
-      std::vector<int> live;  // positions in act of systems stepping
-      for (int a = 0; a < na; a++)
-        if (!stop[a]) live.push_back(a);
-      if (live.empty()) break;
-      const int nl = (int)live.size();
-      std::vector<int> ll(nl);
-      for (int b = 0; b < nl; b++) ll[b] = sl[live[b]];
-      CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, ll.data(), sizeof(int) * nl, cudaMemcpyHostToDevice, st));
-      M(GV(j), GZ(j), nl, dl);
-      o32.apply_A(GZ(j), GW, nl, dl, sc);
-      for (int i = 0; i <= j; i++) {
-        std::vector<double2> h = batch_dot(GW, GV(i), nl, dl);
-        for (int b = 0; b < nl; b++) H[live[b]][(size_t)j * (m + 1) + i] = Z(h[b]);
-        CSEM_CUDA_TRY(cudaMemcpyAsync(cf, h.data(), sizeof(double2) * nl, cudaMemcpyHostToDevice, st));
-        launch_axpy<F32>(n, nl, dl, cf, 1, 1, GV(i), GW, st);
-      }
-      std::vector<double2> hn = batch_dot(GW, GW, nl, dl);
-      std::vector<double2> dv(nl);
-      for (int b = 0; b < nl; b++) {
-        const double hv = std::sqrt(hn[b].x);
-        H[live[b]][(size_t)j * (m + 1) + j + 1] = zc(hv, 0.0);
-        dv[b] = make_double2(hv > 0 ? hv : 1.0, 0.0);
-      }
-      CSEM_CUDA_TRY(cudaMemcpyAsync(cf, dv.data(), sizeof(double2) * nl, cudaMemcpyHostToDevice, st));
-      launch_cdivv<F32>(n, nl, dl, cf, 1, 1, GW, GV(j + 1), st);
-      for (int b = 0; b < nl; b++) {
-        const int a = live[b];
-        zc* col = &H[a][(size_t)j * (m + 1)];
-        for (int i = 0; i < j; i++) {  // earlier rotations
-          const zc t = std::conj(cs[a][i]) * col[i] + sn[a][i] * col[i + 1];
-          col[i + 1] = -sn[a][i] * col[i] + cs[a][i] * col[i + 1];
-          col[i] = t;
+    launch_dot<F32>(GW, GW, n, n, na, dl, partial.as<double2>(), nblk, dots + (size_t)(m + 1) * nsys, this->st);
+    count_launch(), k_gm_begin<<<nb32, 32, 0, this->st>>>(na, dl, st, dots + (size_t)(m + 1) * nsys, gg, coef, m,
+                                                          cycle == 0);
+    launch_cdivv<F32>(n, na, dl, coef, 1, 1, GW, GV(0), this->st);
+    // the m Arnoldi steps and the update of d: one fixed launch sequence for na systems
+    auto steps = [&]() {
+      for (int j = 0; j < m; j++) {
+        M(GV(j), GZ(j), na, dl);
+        o32.apply_A(GZ(j), GW, na, dl, sc);
+        for (int i = 0; i <= j; i++) {  // modified Gram-Schmidt
+          launch_dot<F32>(GW, GV(i), n, n, na, dl, partial.as<double2>(), nblk, dots + (size_t)i * nsys, this->st);
+          launch_axpy<F32>(n, na, dl, dots + (size_t)i * nsys, 1, 1, GV(i), GW, this->st);
         }
-        const double tmp = std::sqrt(std::norm(col[j]) + std::norm(col[j + 1]));
-        if (tmp == 0.0) {
-          stop[a] = 1;
-          continue;
-        }
-        sn[a][j] = col[j + 1].real() / tmp;
-        cs[a][j] = col[j] / tmp;
-        gg[a][j + 1] = -sn[a][j] * gg[a][j];
-        gg[a][j] = std::conj(cs[a][j]) * gg[a][j];
-        col[j] = std::conj(cs[a][j]) * col[j] + sn[a][j] * col[j + 1];
-        steps[a] = j + 1;
-        iters[act[a]] += 1;
-        const double rel = std::abs(gg[a][j + 1]) / beta0[act[a]];
-        if (rel < tol_inner[act[a]] || !(hn[b].x > 0.0)) {
-          stop[a] = 1;
-          done[act[a]] = 1;
-        } else if (iters[act[a]] >= o.niter) {
-          stop[a] = 1;
-        }
+        launch_dot<F32>(GW, GW, n, n, na, dl, partial.as<double2>(), nblk, dots + (size_t)m * nsys, this->st);
+        count_launch(), k_gm_step<<<nb32, 32, 0, this->st>>>(na, dl, st, dots, nsys, H, cs, sn, gg, coef, m, j);
+        launch_cdivv<F32>(n, na, dl, coef, 1, 1, GW, GV(j + 1), this->st);
       }
-    }
-    // d += sum_i y_i z_i, y from the triangular system, per system with its own size
-    int mmax = 0;
-    for (int a = 0; a < na; a++) mmax = std::max(mmax, steps[a]);
-    std::vector<double2> y((size_t)mmax * na, make_double2(0, 0));
-    for (int a = 0; a < na; a++) {
-      const int mm = steps[a];
-      std::vector<zc> yv(mm);
-      for (int i = mm - 1; i >= 0; i--) {
-        zc acc = gg[a][i];
-        for (int k2 = i + 1; k2 < mm; k2++) acc -= H[a][(size_t)k2 * (m + 1) + i] * yv[k2];
-        yv[i] = acc / H[a][(size_t)i * (m + 1) + i];
-      }
-      for (int i = 0; i < mm; i++) y[(size_t)i * na + a] = D2(yv[i]);
-    }
-    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, sl.data(), sizeof(int) * na, cudaMemcpyHostToDevice, st));
-    if (mmax > 0)
-      CSEM_CUDA_TRY(cudaMemcpyAsync(cf, y.data(), sizeof(double2) * y.size(), cudaMemcpyHostToDevice, st));
-    for (int i = 0; i < mmax; i++) launch_axpy<F32>(n, na, dl, cf + (size_t)i * na, 1, 0, GZ(i), GD, st);
+      count_launch(), k_gm_solve<<<nb32, 32, 0, this->st>>>(na, dl, st, H, gg, ycoef, nsys, m);
+      dim3 grd((unsigned)((n + 255) / 256), (unsigned)na);
+      count_launch(), k_gm_update<<<grd, 256, 0, this->st>>>(n, dl, st, ycoef, nsys, GZ(0), N, GD);
+    };
+    run_captured(gm_graphs_[std::make_tuple(na, m, o.preco, 0)], o.graphs, steps);
     CSEM_CUDA_TRY(cudaGetLastError());
+    CSEM_CUDA_TRY(cudaMemcpyAsync(sh.data(), st, sizeof(GmState) * nsys, cudaMemcpyDeviceToHost, this->st));
+    CSEM_CUDA_TRY(cudaStreamSynchronize(this->st));
   }
+  iters.assign(ns, 0);
+  for (int q = 0; q < ns; q++) iters[q] = sh[g[q]].iters;
 }
 
 void MixedBatch::solve_gmres(const std::vector<double>& bn, const double* tol, const MixedOptions& o,
@@ -500,12 +595,13 @@ void MixedBatch::solve_gmres(const std::vector<double>& bn, const double* tol, c
 {
   const int m = std::max(1, o.nrestart);
   const size_t need = sizeof(float2) * (size_t)(2 * m + 4) * nsys * n;
-  if (gm.bytes < need) gm.alloc(need);
+  if (gm.bytes < need) {
+    drop_gmres_graphs();  // they hold the old buffer's addresses
+    gm.alloc(need);
+  }
   // the Z_j are written only by the preconditioner, which leaves boundary entries as
   // they are: they start at zero for this solve (the layout depends on m)
   CSEM_CUDA_TRY(cudaMemsetAsync(gm.p, 0, need, st));
-  const size_t needc = sizeof(double2) * (size_t)(m + 2) * nsys;
-  if (gcoef.bytes < needc) gcoef.alloc(needc);
   const float2* GD = gm.as<float2>() + (size_t)(2 * m + 2) * nsys * n;
   while (!running.empty()) {
     std::vector<double> ti;

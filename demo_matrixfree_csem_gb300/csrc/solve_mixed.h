@@ -1,6 +1,7 @@
 // Batched mixed-precision solver: complex64 inner flexible BiCGStab (LU-SGS or A-phi
 // preconditioned) inside a complex128 defect-correction loop, many systems at once.
 #pragma once
+#include <functional>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -42,7 +43,7 @@ class MixedBatch {
   Ops<F64> o64;
   Ops<F32> o32;
   DevBuf x64, b64, r64, w64, vec32, ks, sc64, sc32, dots, partial, list, rn, srcbuf, chbuf, recbuf, outbuf;
-  DevBuf gm, gcoef;  // GMRES basis (V, Z, w, d, r0) and per-system coefficients
+  DevBuf gm, gstate;  // GMRES basis (V, Z, w, d, r0) and per-system Hessenberg state
   // complex64 FBiCGStab vectors r, r0, p, pp, v, s, t, d (the correction), sh (preconditioned s)
   static constexpr int NVEC32 = 9;
   float2* V(int i) { return vec32.as<float2>() + (size_t)i * nsys * n; }
@@ -66,7 +67,11 @@ class MixedBatch {
     int seen = 0;       // times the combination occurred
     bool failed = false;
   };
-  std::map<std::tuple<int, int, int, int>, Graph> graphs_;
+  std::map<std::tuple<int, int, int, int>, Graph> graphs_, gm_graphs_;
+  // body() launched directly the first time g's combination occurs, as a captured CUDA
+  // graph from the second time on (never while per-operator profiling records events)
+  void run_captured(Graph& g, bool use_graphs, const std::function<void()>& body);
+  void drop_gmres_graphs();  // before the GMRES buffers move
   void start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner);
   int autotune_lusgs(int nact, const int* dlist);  // returns the chosen points per thread
   void outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first, const float2* d = nullptr);
@@ -75,7 +80,6 @@ class MixedBatch {
   // one complex64 flexible GMRES(m) inner solve of A d = r/|r| for the systems g
   void gmres_inner(const std::vector<int>& g, const std::vector<double>& tol_inner, const MixedOptions& o,
                    std::vector<int>& iters);
-  std::vector<double2> batch_dot(const float2* a, const float2* b, int ng, const int* dl);
 };
 
 }  // namespace csem

@@ -92,10 +92,11 @@ def test_tiled_batch_matches_pipelined_batch(gpu, tmp_path):
 
 
 @pytest.mark.parametrize("shape", SHAPES[:3], ids=[f"{s[1]}x{s[2]}x{s[3]}_air{s[5]}" for s in SHAPES[:3]])
-def test_pipelined_prefetch_depths_give_identical_bits(gpu, tmp_path, shape):
+def test_pipelined_prefetch_depths_agree(gpu, tmp_path, shape):
     """The complex64 pipelined sweeps load their operands 1, 2 or 3 march positions ahead
-    (lusgs_prefetch): the same operations on the same values, so the same bits, for
-    every points-per-thread width."""
+    (lusgs_prefetch): the same operations on the same values, for every points-per-thread
+    width. Each depth is its own kernel, and the compiler may contract multiply-adds
+    differently in each, so the bound is 1e-6 relative rather than equal bits."""
     G, ctx, O, _ = _setup(tmp_path, *shape)
     iom = cs.iom_of(0.75)
     x = probe(ctx.lE, shape[0] + 1)
@@ -105,6 +106,7 @@ def test_pipelined_prefetch_depths_give_identical_bits(gpu, tmp_path, shape):
         ref = ctx.lusgs_apply(iom, x, c64=True)
         for pd in (2, 3):
             ctx.set_option("lusgs_prefetch", pd)
-            assert np.array_equal(ctx.lusgs_apply(iom, x, c64=True), ref), (vw, pd)
+            got = ctx.lusgs_apply(iom, x, c64=True)
+            assert relerr(got, ref) <= 1e-6, (vw, pd, relerr(got, ref))
     ctx.set_option("lusgs_prefetch", 1)
     ctx.set_option("lusgs_vw", 0)
