@@ -10,10 +10,9 @@ diagonal is that of div(sigma grad v) and every conductivity comes from the oper
 grid, so the node sweep is an ordinary Gauss-Seidel sweep.
 
 Checked here: the option leaves the reference's behaviour untouched when off; with it
-the preconditioner stays bounded on the bathymetry model; and complex64 GMRES(10) with
-the fixed A-phi inside complex128 defect correction converges to the receivers the
-complex128 BiCGStab + LU-SGS solver gives, to 1e-6 (both stop at tol = 1e-8/f on the
-true residual)."""
+the preconditioner stays bounded on the bathymetry model (complex64 within 1e-4 of
+complex128); and complex64 GMRES(10) with the fixed A-phi runs finite and lowers the
+residual."""
 import tempfile
 
 import numpy as np
@@ -64,29 +63,22 @@ def test_fixed_aphi_is_bounded_on_bathymetry(gpu):
     assert relerr(y_fix32, y_fix) <= 1e-4
 
 
-@pytest.mark.parametrize("model", ["random", "bathymetry"])
-def test_mixed_gmres_with_fixed_aphi_converges(gpu, tmp_path, model):
-    if model == "random":
-        cfg = synthetic.random_small(82, nx=24, ny=20, nz=14, nb=4, airbc=1, n1fft=64, n2fft=64)
-        synthetic.write_config(cfg, str(tmp_path))
-        G = product_grid(str(tmp_path), {k: str(v) for k, v in cfg.params.items()})
-        freqs = np.array([0.5, 1.0], np.float32)
-    else:
-        cfg = synthetic.bathymetry_125()
-        cfg.params["nb"] = 10
-        with tempfile.TemporaryDirectory() as d:
-            G = synthetic.build_grid(cfg, d)
-        freqs = np.array([1.25, 1.25], np.float32)
+def test_mixed_gmres_with_fixed_aphi_stays_finite_and_progresses(gpu, tmp_path):
+    """With the fix, complex64 GMRES(10) with A-phi inside complex128 defect correction
+    runs without overflow and lowers the true residual. It does not converge within a
+    practical budget, however: measured on this model, 9000 inner iterations (3 defect
+    corrections) stopped short of tol = 1e-8/f, and on the bathymetry model as well, where
+    complex128 BiCGStab + LU-SGS converges in 117 iterations; the reference's own A-phi
+    stalls too. The uneven-size batch therefore runs GMRES(10) with LU-SGS
+    (tests/test_gpu_uneven.py)."""
+    cfg = synthetic.random_small(82, nx=24, ny=20, nz=14, nb=4, airbc=1, n1fft=64, n2fft=64)
+    synthetic.write_config(cfg, str(tmp_path))
+    G = product_grid(str(tmp_path), {k: str(v) for k, v in cfg.params.items()})
     ctx = cs.Ctx(G, 1, 0)
+    freqs = np.array([0.5, 1.0], np.float32)
     src = np.repeat(cfg.acq.src[:1, :3], 2, axis=0)
-    src[1, 0] += 300.0 if model == "bathymetry" else 30.0
-    ref = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=64, algopt=1, preco=1, niter=3000, tol=1e-8)
-    assert ref["status"] == ["converged"] * 2
     ctx.set_option("aphi_fix", 1)
-    got = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=32, algopt=2, nrestart=10, preco=3, niter=3000,
-                         tol=1e-8, max_outer=60)
-    print(f"{model}: GMRES(10) + fixed A-phi: status {got['status']}, inner iterations {got['iters'].tolist()}, "
-          f"defect corrections {got['outer'].tolist()}; complex128 BiCGStab + LU-SGS iterations {ref['iters'].tolist()}")
-    assert got["status"] == ["converged"] * 2
-    for q in range(2):
-        assert relerr(got["dcal"][q], ref["dcal"][q]) <= 1e-6, relerr(got["dcal"][q], ref["dcal"][q])
+    got = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=32, algopt=2, nrestart=10, preco=3, niter=200,
+                         tol=1e-8, max_outer=2)
+    assert all(s in ("maxiter", "converged") for s in got["status"]), got["status"]
+    assert np.all(np.isfinite(got["dcal"])) and np.all(got["relres"] < 1.0), got["relres"]
