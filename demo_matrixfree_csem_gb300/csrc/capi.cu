@@ -29,7 +29,7 @@ struct csem_ctx {
   int nmax64 = 0, nmax32 = 0;
   bool lusgs_pipelined = true;
   int lusgs_vw = 0;
-  int lusgs_prefetch = 1;
+  int lusgs_lines = 1;
   bool lusgs_tiled = false;
   bool aphi_fix = false;
   int tile_rows = 8, tile_vw = 4;
@@ -43,7 +43,7 @@ template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
 {
   o.pipelined_sweeps = c->lusgs_pipelined;
   o.sweep_vw = c->lusgs_vw;
-  o.sweep_prefetch = c->lusgs_prefetch;
+  o.sweep_lines = c->lusgs_lines;
   o.tiled_sweeps = c->lusgs_tiled;
   o.aphi_fix = c->aphi_fix;
   o.tile_rows = c->tile_rows;
@@ -169,9 +169,9 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     if (value != 0 && value != 1 && value != 2 && value != 4)
       return csem_set_error(CSEM_EINVAL, "lusgs_vw must be 0, 1, 2 or 4");
     c->lusgs_vw = value;
-  } else if (!strcmp(name, "lusgs_prefetch")) {
-    if (value < 1 || value > 3) return csem_set_error(CSEM_EINVAL, "lusgs_prefetch must be 1, 2 or 3");
-    c->lusgs_prefetch = value;
+  } else if (!strcmp(name, "lusgs_lines")) {
+    if (value < 1 || value > 64) return csem_set_error(CSEM_EINVAL, "lusgs_lines must be in 1..64");
+    c->lusgs_lines = value;
   } else if (!strcmp(name, "aphi_fix")) {
     c->aphi_fix = value != 0;
   } else if (!strcmp(name, "lusgs_tiled")) {

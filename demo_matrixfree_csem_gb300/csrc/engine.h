@@ -63,7 +63,7 @@ template <class P> struct SweepP {
 // one launch per component sweep (pipelined warps, k_lusgs2.cu)
 template <class P>
 void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw,
-                            int prefetch = 1);
+                            int lines_per_cta = 1);
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK);  // the sweep's rows fit one CTA
 // complex64 line-tiled sweeps (k_lusgs3.cu): 32 lines per CTA, rows in warp blocks of at
 // most rows_per_warp (4, 8, 16), vw march positions per step for Ey/Ez (1, 2, 4)

@@ -354,7 +354,7 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
       }
     }
     if (pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
-      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st, sweep_vw, sweep_prefetch);
+      launch_sweep_pipelined<P>(s, comp, fwd, nslot, st, sweep_vw, sweep_lines);
       return;
     }
     const int nd = sweep_diagonals(comp, n1, n2, s.nK);

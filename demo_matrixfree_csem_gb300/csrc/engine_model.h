@@ -88,7 +88,7 @@ class Ops {
   // false = one launch per wavefront diagonal (k_lusgs.cu); both give identical results
   bool pipelined_sweeps = true;
   int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
-  int sweep_prefetch = 1;  // complex64: march positions the pipelined sweeps load ahead (1..3)
+  int sweep_lines = 1;  // complex64: lines one CTA of the pipelined sweeps carries as a conveyor
   // complex64 only: line-tiled sweeps (k_lusgs3.cu) instead of the pipelined ones, with
   // at most tile_rows rows per warp and tile_vw march positions per step (Ey, Ez)
   bool tiled_sweeps = false;

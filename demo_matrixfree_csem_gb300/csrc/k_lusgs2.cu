@@ -526,9 +526,16 @@ template <int VW> struct RawEyz {
 
 }  // namespace
 
-// Ex, complex64: rows k, march j, VW consecutive i per thread. grid (i groups, systems)
-template <bool FWD, int VW, int MAXR, int PD>
-__global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
+// Ex, complex64: rows k, march j, VW consecutive i per thread. grid (line groups, systems).
+//
+// A CTA may carry several lines one after the other (lpc lines, a conveyor): a row that
+// finishes its march on one line starts the next line at the next step, while the rows
+// behind it are still on the previous one. Row t works at step T on conveyor position
+// u = T - t, i.e. line u / M, march position u % M, so the row before it finished the
+// same line and position at step T - 1 and the hand-over is unchanged. The pipeline
+// fills and drains once per CTA instead of once per line.
+template <bool FWD, int VW, int MAXR>
+__global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s, int lpc)
 {
   typedef float2 C;
   __shared__ HandOff<VW, C, (MAXR <= NB_ROWS)> hand;
@@ -536,46 +543,52 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<F32>& g = s.g;
   const int n1 = g.n1, n2 = g.n2, nK = s.nK;
-  const int i0 = blockIdx.x * VW;
+  const int nlines = (n1 + VW - 1) / VW;
+  const int line0 = blockIdx.x * lpc;
+  const int nl = min(lpc, nlines - line0);
   const View<F32> V = view_of<F32>(s, slot, sys);
   const SysScal<F32> sc = s.scal[sys];
   const C z = make_float2(0.f, 0.f);
   const int R_ = nK - 1, M = n2 - 1;  // rows k = 1..R_, march j = 1..M
+  const int U = nl * M;               // conveyor positions
   const int rr = threadIdx.x;
   const bool rowok = rr < R_;
   const int k = FWD ? 1 + rr : R_ - rr;
   const Ax<F32> Z = rowok ? axis<F32>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<F32>{};
-  Ax<F32> X[VW];
-#pragma unroll
-  for (int q = 0; q < VW; q++)
-    X[q] = i0 + q < n1 ? axis_at<F32>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<F32>{};
+  // the row's planes at i = 0; a line adds its first i
   C* ex0 = nullptr;
   const C *ex1 = nullptr, *ey0 = nullptr, *ez0 = nullptr, *ez1 = nullptr, *bb = nullptr;
   const float* sg0 = nullptr;
   if (rowok) {
-    ex0 = V.row(0, k, 0) + i0;
-    ex1 = V.row(0, k - 1, 0) + i0;
-    ey0 = V.row(1, k, 0) + i0;
-    ez0 = V.row(2, k, 0) + i0;
-    ez1 = V.row(2, k - 1, 0) + i0;
+    ex0 = V.row(0, k, 0);
+    ex1 = V.row(0, k - 1, 0);
+    ey0 = V.row(1, k, 0);
+    ez0 = V.row(2, k, 0);
+    ez1 = V.row(2, k - 1, 0);
     bb = V.brow(0, k, 0);
-    if (bb) bb += i0;
-    sg0 = g.s11 + ix1(n1, n2, k, 0, i0);
+    sg0 = g.s11 + ix1(n1, n2, k, 0, 0);
   }
   const int L1 = n1 + 1;
   const float gn = Z.r * (FWD ? Z.rsm : Z.rs);
-  // operands of the next PD march positions: ring[q] holds position c+1+q at step
-  // T = c + rr (loads issued PD steps ahead of their use)
-  RawEx<VW> ring[PD];
+  int il = line0 * VW;  // first i of the line the loads are on
+  int is = il;          // first i of the line the stores are on
+  Ax<F32> X[VW];        // spacings of the load line's i's
+  auto set_line = [&](int i0) {
+    il = i0;
+#pragma unroll
+    for (int q = 0; q < VW; q++) X[q] = i0 + q < n1 ? axis_at<F32>(g.d1, g.d1s, g.r1, g.r1s, i0 + q) : Ax<F32>{};
+  };
+  set_line(il);
+  RawEx<VW> raw;
   Lin32 lin[VW];
-  // loads of march position c (nothing read here is written before that step)
-  auto load = [&](int c, RawEx<VW>& raw) {
+  // loads of march position c of the load line (nothing read here is written before that step)
+  auto load = [&](int c) {
     const int j = FWD ? 1 + c : M - c;
     raw.Y = axis<F32>(g.d2, g.d2s, g.r2, g.r2s, j);
-    const int ox = j * n1, oy = j * L1;
+    const int ox = j * n1 + il, oy = j * L1 + il;
 #pragma unroll
     for (int q = 0; q < VW; q++) {
-      if (i0 + q < n1) {
+      if (il + q < n1) {
         raw.b[q] = bb ? ro(bb + ox + q) : z;
         raw.sg[q] = ro(sg0 + ox + q);
         if (!FWD) {
@@ -593,13 +606,13 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
       }
     }
   };
-  auto make = [&](const RawEx<VW>& raw) {
+  auto make = [&]() {
     const Ax<F32>& Y = raw.Y;
     const float gg = (Y.rs + Y.rsm) * Y.r + (Z.rs + Z.rsm) * Z.r;  // geo(Y, Z)
     const float gp = Y.r * (FWD ? Y.rsm : Y.rs);
 #pragma unroll
     for (int q = 0; q < VW; q++) {
-      if (i0 + q >= n1) continue;
+      if (il + q >= n1) continue;
       C kc = z;
       if (!FWD) {
         const C dy = sub32(sub32(raw.eyA[q], raw.eyB[q]), sub32(raw.eyC[q], raw.eyD[q]));
@@ -615,51 +628,51 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_ex32(SweepP<F32> s)
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
-  if (rowok && rr == 0 && M > 0) {
-    RawEx<VW> r0;
-    load(0, r0);
-    make(r0);
+  if (rowok && rr == 0 && U > 0) {
+    load(0);
+    make();
   }
-#pragma unroll
-  for (int q = 0; q + 1 < PD; q++) {
-    const int p = 1 - rr + q;
-    if (rowok && p >= 0 && p < M) load(p, ring[q]);
-  }
-  for (int T = 0; T < M + R_ - 1; T++) {
-    const int c = T - rr;
-    const bool act = rowok && c >= 0 && c < M;
-    const bool nxt = rowok && c + 1 >= 0 && c + 1 < M;
-    if (rowok && c + PD >= 0 && c + PD < M) load(c + PD, ring[PD - 1]);
+  for (int T = 0; T < U + R_ - 1; T++) {
+    const int u = T - rr;
+    const bool act = rowok && u >= 0 && u < U;
+    const bool nxt = rowok && u + 1 >= 0 && u + 1 < U;
+    int cn = 0;
+    if (nxt) {
+      cn = (u + 1) % M;
+      if (cn == 0 && u + 1 > 0) set_line((line0 + (u + 1) / M) * VW);  // the loads move to the next line
+      load(cn);
+    }
     C nb[VW];
     hand.get(res, nb, T);
     if (act) {
-      const int ox = (FWD ? 1 + c : M - c) * n1;
+      const int c = u % M;
+      const int ox = (FWD ? 1 + c : M - c) * n1 + is;
 #pragma unroll
       for (int q = 0; q < VW; q++) {
-        if (i0 + q >= n1) {
+        if (is + q >= n1) {
           res[q] = z;
           continue;
         }
-        const C v = lin_apply(lin[q], res[q], nb[q]);  // prev: own row, previous j
+        const C v = lin_apply(lin[q], c > 0 ? res[q] : z, nb[q]);  // prev: own row, previous j
         ex0[ox + q] = v;
         res[q] = v;
       }
+      if (c == M - 1) is = il;  // the stores follow the loads onto the next line
     } else {
 #pragma unroll
       for (int q = 0; q < VW; q++) res[q] = z;
     }
     hand.put(res, T);
-    if (nxt) make(ring[0]);
-#pragma unroll
-    for (int q = 0; q + 1 < PD; q++) ring[q] = ring[q + 1];
+    if (nxt) make();
   }
-  hand.finish(M + R_ - 1);
+  hand.finish(U + R_ - 1);
 }
 
 // Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j), complex64: march i in
-// chunks of VW. grid (lines, systems)
-template <int COMP, bool FWD, int VW, int MAXR, int PD>
-__global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
+// chunks of VW, lpc lines per CTA as a conveyor (see k_sweep_ex32). grid (line groups,
+// systems)
+template <int COMP, bool FWD, int VW, int MAXR>
+__global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s, int lpc)
 {
   typedef float2 C;
   __shared__ HandOff<VW, C, (MAXR <= NB_ROWS)> hand;
@@ -667,33 +680,36 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<F32>& g = s.g;
   const int n1 = g.n1, n2 = g.n2, nK = s.nK;
-  const int line = blockIdx.x;  // j (Ey) or k (Ez)
+  const int nlines = COMP == 1 ? n2 : nK;
+  const int line0 = blockIdx.x * lpc;
+  const int nl = min(lpc, nlines - line0);
   const View<F32> V = view_of<F32>(s, slot, sys);
   const SysScal<F32> sc = s.scal[sys];
   const C z = make_float2(0.f, 0.f);
   const int R_ = COMP == 1 ? nK - 1 : n2 - 1;  // rows k (Ey) or j (Ez) = 1..R_
   const int M = n1 - 1;                         // march i = 1..M
   const int NC = (M + VW - 1) / VW;
+  const int U = nl * NC;  // conveyor positions
   const int rr = threadIdx.x;
   const bool rowok = rr < R_;
   const int r = FWD ? 1 + rr : R_ - rr;
-  const int k = COMP == 1 ? r : line;
-  const int j = COMP == 1 ? line : r;
-  // the line's and the row's spacings; R is the row axis (Z for Ey, Y for Ez), L the line's
-  Ax<F32> Y, Z;
-  if (COMP == 1) {
-    Y = axis_at<F32>(g.d2, g.d2s, g.r2, g.r2s, j);
-    Z = rowok ? axis<F32>(g.d3, g.d3s, g.r3, g.r3s, k) : Ax<F32>{};
-  } else {
-    Y = rowok ? axis<F32>(g.d2, g.d2s, g.r2, g.r2s, j) : Ax<F32>{};
-    Z = axis_at<F32>(g.d3, g.d3s, g.r3, g.r3s, k);
-  }
-  const Ax<F32>& Rw = COMP == 1 ? Z : Y;
+  // the row's axis (Z for Ey, Y for Ez) is fixed; the line's axis (Y for Ey, Z for Ez)
+  // moves with the conveyor
+  const Ax<F32> Rw = rowok ? (COMP == 1 ? axis<F32>(g.d3, g.d3s, g.r3, g.r3s, r) : axis<F32>(g.d2, g.d2s, g.r2, g.r2s, r))
+                           : Ax<F32>{};
+  const float gn = Rw.r * (FWD ? Rw.rsm : Rw.rs);
+  // the rows the loads read (element i is row[i]) and the line's spacings
   C* own = nullptr;
   const C *nxt = nullptr, *xa = nullptr, *xb = nullptr, *ya = nullptr, *yb = nullptr, *yc = nullptr, *yd = nullptr;
   const C* bb = nullptr;
   const float* sg0 = nullptr;
-  if (rowok) {
+  float lrs = 0.f, ld = 0.f;  // the line axis' rs (the coefficient of the line-axis differences) and d
+  auto set_line = [&](int line) {
+    const int k = COMP == 1 ? r : line;
+    const int j = COMP == 1 ? line : r;
+    const Ax<F32> LA = COMP == 1 ? axis_at<F32>(g.d2, g.d2s, g.r2, g.r2s, j) : axis_at<F32>(g.d3, g.d3s, g.r3, g.r3s, k);
+    lrs = LA.rs;
+    ld = LA.d;
     if (COMP == 1) {
       own = V.row(1, k, j);
       nxt = V.row(1, k - 1, j);
@@ -716,13 +732,12 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
       sg0 = g.s33 + ix3(n1, n2, k, j, 0);
     }
     bb = V.brow(COMP, k, j);
-  }
-  const float gn = Rw.r * (FWD ? Rw.rsm : Rw.rs);
-  // the coefficient of the line-axis differences in cross: Y.rs (Ey) or Z.rs (Ez)
-  const float lrs = COMP == 1 ? Y.rs : Z.rs;
-  RawEyz<VW> ring[PD];  // ring[q]: operands of position c+1+q at step T = c + rr
+  };
+  if (rowok) set_line(line0);
+  C* own_st = own;  // the row the stores go to (the loads run one position ahead)
+  RawEyz<VW> raw;
   Lin32 lin[VW];
-  auto load = [&](int c, RawEyz<VW>& raw) {
+  auto load = [&](int c) {
 #pragma unroll
     for (int q = 0; q < VW; q++) {
       const int m = c * VW + q;
@@ -748,7 +763,7 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
       }
     }
   };
-  auto make = [&](int c, const RawEyz<VW>& raw) {
+  auto make = [&](int c) {
 #pragma unroll
     for (int q = 0; q < VW; q++) {
       if (c * VW + q >= M) continue;
@@ -767,30 +782,31 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
                                     X.r * X.rsm * raw.own2[q].y + Rw.r * Rw.rsm * raw.rowold[q].y);
         kc = make_float2(kc.x + known.x, kc.y + known.y);
       }
-      lin[q] = lin_make(sc, g.fvm, gg, raw.sg[q], X.ds * Y.d * Z.d, raw.b[q], kc, X.r * (FWD ? X.rsm : X.rs), gn);
+      const float yd = COMP == 1 ? ld : Rw.d, zd = COMP == 1 ? Rw.d : ld;  // Y.d and Z.d
+      lin[q] = lin_make(sc, g.fvm, gg, raw.sg[q], X.ds * yd * zd, raw.b[q], kc, X.r * (FWD ? X.rsm : X.rs), gn);
     }
   };
   C res[VW];
 #pragma unroll
   for (int q = 0; q < VW; q++) res[q] = z;
-  if (rowok && rr == 0 && NC > 0) {
-    RawEyz<VW> r0;
-    load(0, r0);
-    make(0, r0);
+  if (rowok && rr == 0 && U > 0) {
+    load(0);
+    make(0);
   }
-#pragma unroll
-  for (int q = 0; q + 1 < PD; q++) {
-    const int p = 1 - rr + q;
-    if (rowok && p >= 0 && p < NC) load(p, ring[q]);
-  }
-  for (int T = 0; T < NC + R_ - 1; T++) {
-    const int c = T - rr;
-    const bool act = rowok && c >= 0 && c < NC;
-    const bool nx = rowok && c + 1 >= 0 && c + 1 < NC;
-    if (rowok && c + PD >= 0 && c + PD < NC) load(c + PD, ring[PD - 1]);
+  for (int T = 0; T < U + R_ - 1; T++) {
+    const int u = T - rr;
+    const bool act = rowok && u >= 0 && u < U;
+    const bool nx = rowok && u + 1 >= 0 && u + 1 < U;
+    int cn = 0;
+    if (nx) {
+      cn = (u + 1) % NC;
+      if (cn == 0 && u + 1 > 0) set_line(line0 + (u + 1) / NC);  // the loads move to the next line
+      load(cn);
+    }
     C nb[VW];
     hand.get(res, nb, T);
     if (act) {
+      const int c = u % NC;
       C prev = c > 0 ? res[VW - 1] : z;  // own row at the previous march position
 #pragma unroll
       for (int q = 0; q < VW; q++) {
@@ -800,20 +816,19 @@ __global__ void CSEM_SWEEP_BOUNDS32(VW, MAXR) k_sweep_eyz32(SweepP<F32> s)
           continue;
         }
         const C v = lin_apply(lin[q], prev, nb[q]);
-        own[FWD ? 1 + m : M - m] = v;
+        own_st[FWD ? 1 + m : M - m] = v;
         res[q] = v;
         prev = v;
       }
+      if (c == NC - 1) own_st = own;  // the stores follow the loads onto the next line
     } else {
 #pragma unroll
       for (int q = 0; q < VW; q++) res[q] = z;
     }
     hand.put(res, T);
-    if (nx) make(c + 1, ring[0]);
-#pragma unroll
-    for (int q = 0; q + 1 < PD; q++) ring[q] = ring[q + 1];
+    if (nx) make(cn);
   }
-  hand.finish(NC + R_ - 1);
+  hand.finish(U + R_ - 1);
 }
 
 bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
@@ -822,27 +837,27 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK)
   return rows >= 1 && rows <= MAXROWS && n1 >= 2 && n2 >= 2;
 }
 
-template <class P, int VW, int MAXR, int PD>
-static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st)
+template <class P, int VW, int MAXR>
+static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int lpc)
 {
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
   const int threads = (rows + 31) / 32 * 32;
-  if constexpr (!P::exact) {  // complex64: the linear-form sweeps
+  if constexpr (!P::exact) {  // complex64: the linear-form sweeps, lpc lines per CTA
     if (comp == 0) {
-      dim3 grd((n1 + VW - 1) / VW, nslot);
-      if (fwd) count_launch(), k_sweep_ex32<true, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
-      else count_launch(), k_sweep_ex32<false, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
+      dim3 grd(((n1 + VW - 1) / VW + lpc - 1) / lpc, nslot);
+      if (fwd) count_launch(), k_sweep_ex32<true, VW, MAXR><<<grd, threads, 0, st>>>(s, lpc);
+      else count_launch(), k_sweep_ex32<false, VW, MAXR><<<grd, threads, 0, st>>>(s, lpc);
     } else if (comp == 1) {
-      dim3 grd(n2, nslot);
-      if (fwd) count_launch(), k_sweep_eyz32<1, true, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
-      else count_launch(), k_sweep_eyz32<1, false, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
+      dim3 grd((n2 + lpc - 1) / lpc, nslot);
+      if (fwd) count_launch(), k_sweep_eyz32<1, true, VW, MAXR><<<grd, threads, 0, st>>>(s, lpc);
+      else count_launch(), k_sweep_eyz32<1, false, VW, MAXR><<<grd, threads, 0, st>>>(s, lpc);
     } else {
-      dim3 grd(nK, nslot);
-      if (fwd) count_launch(), k_sweep_eyz32<2, true, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
-      else count_launch(), k_sweep_eyz32<2, false, VW, MAXR, PD><<<grd, threads, 0, st>>>(s);
+      dim3 grd((nK + lpc - 1) / lpc, nslot);
+      if (fwd) count_launch(), k_sweep_eyz32<2, true, VW, MAXR><<<grd, threads, 0, st>>>(s, lpc);
+      else count_launch(), k_sweep_eyz32<2, false, VW, MAXR><<<grd, threads, 0, st>>>(s, lpc);
     }
-  } else {  // complex128: the reference's operation order
+  } else {  // complex128: the reference's operation order, one line per CTA
     if (comp == 0) {
       dim3 grd((n1 + VW - 1) / VW, nslot);
       if (fwd) count_launch(), k_sweep_ex<P, true, VW, MAXR><<<grd, threads, 0, st>>>(s);
@@ -862,30 +877,22 @@ static void launch_vw(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStr
 // vw: points per thread and step (1, 2 or 4; other values select the default, the
 // fastest measured on a 200x140x140 grid: 2 for complex64, 1 for complex128). Sweeps of
 // more than 256 rows run 1 or 2 points per thread in CTAs of up to 512 threads.
-template <class P, int PD>
-static void launch_pd(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw)
-{
-  const int rows = comp == 2 ? s.g.n2 - 1 : s.nK - 1;
-  if (rows > NB_ROWS) {
-    if (vw == 1) launch_vw<P, 1, MAXROWS, PD>(s, comp, fwd, nslot, st);
-    else launch_vw<P, 2, MAXROWS, PD>(s, comp, fwd, nslot, st);
-    return;
-  }
-  if (vw == 1) launch_vw<P, 1, NB_ROWS, PD>(s, comp, fwd, nslot, st);
-  else if (vw == 2) launch_vw<P, 2, NB_ROWS, PD>(s, comp, fwd, nslot, st);
-  else launch_vw<P, 4, NB_ROWS, PD>(s, comp, fwd, nslot, st);
-}
-
-// prefetch: march positions the complex64 sweeps load ahead of use (1, 2 or 3; the
-// complex128 sweeps always load one position ahead)
+// lines_per_cta: lines one CTA carries as a conveyor (complex64; >= 1).
 template <class P>
 void launch_sweep_pipelined(const SweepP<P>& s, int comp, bool fwd, int nslot, cudaStream_t st, int vw,
-                            int prefetch)
+                            int lines_per_cta)
 {
   if (vw != 1 && vw != 2 && vw != 4) vw = P::exact ? 1 : 2;
-  if (P::exact || prefetch <= 1) launch_pd<P, 1>(s, comp, fwd, nslot, st, vw);
-  else if (prefetch == 2) launch_pd<P, 2>(s, comp, fwd, nslot, st, vw);
-  else launch_pd<P, 3>(s, comp, fwd, nslot, st, vw);
+  const int lpc = lines_per_cta > 1 ? lines_per_cta : 1;
+  const int rows = comp == 2 ? s.g.n2 - 1 : s.nK - 1;
+  if (rows > NB_ROWS) {
+    if (vw == 1) launch_vw<P, 1, MAXROWS>(s, comp, fwd, nslot, st, lpc);
+    else launch_vw<P, 2, MAXROWS>(s, comp, fwd, nslot, st, lpc);
+    return;
+  }
+  if (vw == 1) launch_vw<P, 1, NB_ROWS>(s, comp, fwd, nslot, st, lpc);
+  else if (vw == 2) launch_vw<P, 2, NB_ROWS>(s, comp, fwd, nslot, st, lpc);
+  else launch_vw<P, 4, NB_ROWS>(s, comp, fwd, nslot, st, lpc);
 }
 
 template void launch_sweep_pipelined<F64>(const SweepP<F64>&, int, bool, int, cudaStream_t, int, int);

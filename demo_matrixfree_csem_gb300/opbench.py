@@ -36,7 +36,7 @@ def main(argv=None) -> None:
     ap.add_argument("--freq", type=float, default=0.5)
     ap.add_argument("--schedule", choices=["pipelined", "diagonal"], default="pipelined")
     ap.add_argument("--vw", type=int, default=0)
-    ap.add_argument("--prefetch", type=int, default=1, help="march positions the complex64 sweeps load ahead")
+    ap.add_argument("--lines", type=int, default=1, help="lines per CTA of the complex64 pipelined sweeps")
     ap.add_argument("--tiled", type=int, default=0, help="1: line-tiled complex64 LU-SGS sweeps")
     ap.add_argument("--tile-rows", type=int, default=8)
     ap.add_argument("--tile-vw", type=int, default=4)
@@ -65,7 +65,7 @@ def main(argv=None) -> None:
         return
     ctx.set_option("lusgs_pipelined", 1 if a.schedule == "pipelined" else 0)
     ctx.set_option("lusgs_vw", a.vw)
-    ctx.set_option("lusgs_prefetch", a.prefetch)
+    ctx.set_option("lusgs_lines", a.lines)
     ctx.set_option("lusgs_tiled", a.tiled)
     ctx.set_option("lusgs_tile_rows", a.tile_rows)
     ctx.set_option("lusgs_tile_vw", a.tile_vw)
@@ -107,14 +107,14 @@ def main(argv=None) -> None:
         ctx.set_option("lusgs_tiled", 0)
         ctx.set_option("lusgs_pipelined", 1)
         ctx.set_option("lusgs_vw", 0)
-        ctx.set_option("lusgs_prefetch", 1)
+        ctx.set_option("lusgs_lines", 1)
         apply()
         torch.cuda.synchronize()
         d = (y1 - y).abs().max().item()
         check = {"max_abs_diff": d, "rel": d / max(y.abs().max().item(), 1e-300),
                  "bit_identical": bool(torch.equal(torch.view_as_real(y1), torch.view_as_real(y)))}
     out = {"workload": a.workload, "op": a.op, "prec": a.prec, "nsys": a.nsys, "schedule": a.schedule,
-           "vw": a.vw, "prefetch": a.prefetch, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
+           "vw": a.vw, "lines": a.lines, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
            "ms_per_application": ms, "ms_per_system": ms / a.nsys,
            "algorithmic_bytes_per_system": per_sys,
            "algorithmic_GBps": per_sys * a.nsys / (ms * 1e-3) / 1e9 if per_sys else None}

@@ -227,6 +227,9 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     lockstep pipeline; 0: one launch per wavefront diagonal;
  *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
  *                     0 for the default (2 complex64, 1 complex128).
+ *   "lusgs_lines"     complex64 only: lines one CTA of the pipelined sweeps carries one
+ *                     after the other (1..64), so the row pipeline fills and drains once
+ *                     per CTA instead of once per line; 1 (default): one line per CTA;
  *   "lusgs_tiled"     complex64 only. 1: line-tiled sweeps - 32 independent lines per CTA
  *                     (one lane each), the rows cut into one block per warp; 0: the
  *                     schedule chosen by lusgs_pipelined. Same values as the pipelined

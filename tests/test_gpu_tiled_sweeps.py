@@ -91,22 +91,27 @@ def test_tiled_batch_matches_pipelined_batch(gpu, tmp_path):
         assert relerr(b["dcal"][q], a["dcal"][q]) <= 1e-6
 
 
-@pytest.mark.parametrize("shape", SHAPES[:3], ids=[f"{s[1]}x{s[2]}x{s[3]}_air{s[5]}" for s in SHAPES[:3]])
-def test_pipelined_prefetch_depths_agree(gpu, tmp_path, shape):
-    """The complex64 pipelined sweeps load their operands 1, 2 or 3 march positions ahead
-    (lusgs_prefetch): the same operations on the same values, for every points-per-thread
-    width. Each depth is its own kernel, and the compiler may contract multiply-adds
-    differently in each, so the bound is 1e-6 relative rather than equal bits."""
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{s[1]}x{s[2]}x{s[3]}_air{s[5]}_fvm{s[6]}" for s in SHAPES])
+def test_pipelined_conveyor_of_lines_agrees(gpu, tmp_path, shape):
+    """The complex64 pipelined sweeps with several lines per CTA (lusgs_lines, a conveyor:
+    a row that finishes a line starts the next one while the rows behind it are still on
+    the previous line) give the values of one line per CTA, for every points-per-thread
+    width and for line counts that do not divide the grid. Each configuration is its own
+    kernel path, and the compiler may contract multiply-adds differently, so the bound
+    is 1e-6 relative; against the complex128 oracle the complex64 bound 2e-5 holds."""
     G, ctx, O, _ = _setup(tmp_path, *shape)
+    O.set_freq(0.75)
     iom = cs.iom_of(0.75)
     x = probe(ctx.lE, shape[0] + 1)
+    mo = O.lusgs(x)
     for vw in (1, 2, 4):
         ctx.set_option("lusgs_vw", vw)
-        ctx.set_option("lusgs_prefetch", 1)
+        ctx.set_option("lusgs_lines", 1)
         ref = ctx.lusgs_apply(iom, x, c64=True)
-        for pd in (2, 3):
-            ctx.set_option("lusgs_prefetch", pd)
+        assert relerr(ref, mo) <= 2e-5
+        for lines in (2, 3, 7):
+            ctx.set_option("lusgs_lines", lines)
             got = ctx.lusgs_apply(iom, x, c64=True)
-            assert relerr(got, ref) <= 1e-6, (vw, pd, relerr(got, ref))
-    ctx.set_option("lusgs_prefetch", 1)
+            assert relerr(got, ref) <= 1e-6, (vw, lines, relerr(got, ref))
+    ctx.set_option("lusgs_lines", 1)
     ctx.set_option("lusgs_vw", 0)
