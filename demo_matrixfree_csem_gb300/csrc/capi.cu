@@ -30,6 +30,7 @@ struct csem_ctx {
   bool lusgs_pipelined = true;
   int lusgs_vw = 0;
   int lusgs_lines = 1;
+  int stencil_by = 8, stencil_ctas = 4;
   bool lusgs_tiled = false;
   bool aphi_fix = false;
   int tile_rows = 8, tile_vw = 4;
@@ -44,6 +45,8 @@ template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
   o.pipelined_sweeps = c->lusgs_pipelined;
   o.sweep_vw = c->lusgs_vw;
   o.sweep_lines = c->lusgs_lines;
+  o.stencil_by = c->stencil_by;
+  o.stencil_ctas = c->stencil_ctas;
   o.tiled_sweeps = c->lusgs_tiled;
   o.aphi_fix = c->aphi_fix;
   o.tile_rows = c->tile_rows;
@@ -169,6 +172,12 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     if (value != 0 && value != 1 && value != 2 && value != 4)
       return csem_set_error(CSEM_EINVAL, "lusgs_vw must be 0, 1, 2 or 4");
     c->lusgs_vw = value;
+  } else if (!strcmp(name, "stencil_by")) {
+    if (value != 4 && value != 8 && value != 16) return csem_set_error(CSEM_EINVAL, "stencil_by must be 4, 8 or 16");
+    c->stencil_by = value;
+  } else if (!strcmp(name, "stencil_ctas")) {
+    if (value < 1 || value > 16) return csem_set_error(CSEM_EINVAL, "stencil_ctas must be in 1..16");
+    c->stencil_ctas = value;
   } else if (!strcmp(name, "lusgs_lines")) {
     if (value < 1 || value > 64) return csem_set_error(CSEM_EINVAL, "lusgs_lines must be in 1..64");
     c->lusgs_lines = value;

@@ -10,7 +10,7 @@ namespace csem {
 template <class P>
 void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
                  const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
-                 cudaStream_t st);
+                 cudaStream_t st, int by = 8, int ctas_per_sm = 4);
 template <class P>
 void launch_hz0(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* out,
                 int nsys, const int* sys_list, cudaStream_t st);

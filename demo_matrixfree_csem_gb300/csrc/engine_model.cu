@@ -315,10 +315,10 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
       launch_air_scatter<P>(a, K2.as<C>(), ghx.as<C>(), ghy.as<C>(), nslot, st);
     }
     ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
-    launch_fdfd<P>(g, sc, X, Y, ghx.as<C>(), ghy.as<C>(), nslot, sys_list, st);
+    launch_fdfd<P>(g, sc, X, Y, ghx.as<C>(), ghy.as<C>(), nslot, sys_list, st, stencil_by, stencil_ctas);
   } else {
     ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
-    launch_fdfd<P>(g, sc, X, Y, nullptr, nullptr, nslot, sys_list, st);
+    launch_fdfd<P>(g, sc, X, Y, nullptr, nullptr, nslot, sys_list, st, stencil_by, stencil_ctas);
   }
 }
 

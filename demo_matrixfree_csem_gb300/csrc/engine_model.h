@@ -89,6 +89,8 @@ class Ops {
   bool pipelined_sweeps = true;
   int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
   int sweep_lines = 1;  // complex64: lines one CTA of the pipelined sweeps carries as a conveyor
+  int stencil_by = 8;    // stencil tile: output rows per CTA (4, 8, 16)
+  int stencil_ctas = 4;  // stencil z-blocks: CTAs per SM the plane chunks aim for
   // complex64 only: line-tiled sweeps (k_lusgs3.cu) instead of the pipelined ones, with
   // at most tile_rows rows per warp and tile_vw march positions per step (Ey, Ez)
   bool tiled_sweeps = false;

@@ -233,19 +233,19 @@ __global__ void k_hz0(GridP<P> g, const SysScal<P>* __restrict__ scal, const typ
   out[(size_t)slot * g.n1 * g.n2 + i + (long)g.n1 * j] = hz;
 }
 
-template <class P>
-void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
-                 const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
-                 cudaStream_t st)
+// by: output rows per CTA (4, 8 or 16; other values: 8); ctas_per_sm: how many CTAs per
+// SM the grid aims for when it splits the planes into chunks (other than 1..16: 4), which
+// sets the z-block depth. Neither changes any result: every output takes the same
+// operands in the same operations.
+template <class P, int BY>
+static void launch_fdfd_by(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
+                           const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
+                           cudaStream_t st, int ctas_per_sm)
 {
-#ifndef CSEM_FDFD_BY
-#define CSEM_FDFD_BY 8
-#endif
-  constexpr int BY = CSEM_FDFD_BY;  // output rows per CTA (a build may set others to try)
   dim3 blk(32, BY + 1);
   const int gx = (g.n1 + 1 + 30) / 31, gy = (g.n2 + 1 + BY - 1) / BY;
   const long base = (long)gx * gy * nsys;
-  // split the planes into chunks until about four CTAs per SM are in the grid
+  // split the planes into chunks until about ctas_per_sm CTAs per SM are in the grid
   static int sms[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -254,7 +254,7 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
     (void)cudaGetLastError();
     sms[dev] = 152;
   }
-  int nkc = (int)((4L * sms[dev] + base - 1) / base);
+  int nkc = (int)(((long)ctas_per_sm * sms[dev] + base - 1) / base);
   const int maxc = (g.n3 + 1) / 8 > 0 ? (g.n3 + 1) / 8 : 1;  // chunks of at least 8 planes
   if (nkc > maxc) nkc = maxc;
   if (nkc < 1) nkc = 1;
@@ -262,6 +262,17 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
   nkc = (g.n3 + 1 + kchunk - 1) / kchunk;
   dim3 grd(gx, gy, nsys * nkc);
   count_launch(), k_fdfd<P, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
+}
+
+template <class P>
+void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
+                 const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
+                 cudaStream_t st, int by, int ctas_per_sm)
+{
+  if (ctas_per_sm < 1 || ctas_per_sm > 16) ctas_per_sm = 4;
+  if (by == 4) launch_fdfd_by<P, 4>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm);
+  else if (by == 16) launch_fdfd_by<P, 16>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm);
+  else launch_fdfd_by<P, 8>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm);
 }
 
 template <class P>
@@ -274,9 +285,9 @@ void launch_hz0(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* 
 }
 
 template void launch_fdfd<F64>(const GridP<F64>&, const SysScal<F64>*, const double2*, double2*,
-                               const double2*, const double2*, int, const int*, cudaStream_t);
+                               const double2*, const double2*, int, const int*, cudaStream_t, int, int);
 template void launch_fdfd<F32>(const GridP<F32>&, const SysScal<F32>*, const float2*, float2*,
-                               const float2*, const float2*, int, const int*, cudaStream_t);
+                               const float2*, const float2*, int, const int*, cudaStream_t, int, int);
 template void launch_hz0<F64>(const GridP<F64>&, const SysScal<F64>*, const double2*, double2*, int,
                               const int*, cudaStream_t);
 template void launch_hz0<F32>(const GridP<F32>&, const SysScal<F32>*, const float2*, float2*, int,

@@ -223,41 +223,72 @@ void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rn
   CSEM_CUDA_TRY(cudaMemcpyAsync(rn.p, rnorm.data(), sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
 }
 
-// Autotuner of the complex64 LU-SGS schedule: applies the preconditioner to the batch's
-// current vectors once per candidate (points per thread 1, 2, 4 of the lockstep sweeps)
-// after one untimed application each, times it with CUDA events on the solver's stream,
-// and keeps the fastest for the rest of this batch. The scratch vector it writes is
-// overwritten before use by the solve.
+// Autotuner of the complex64 kernel shapes, on the batch's current vectors: each
+// candidate is applied once untimed and once timed with CUDA events on the solver's
+// stream, and the fastest is kept for the rest of this batch.
+//  - LU-SGS: points per thread and step of the pipelined sweeps (1, 2, 4) x lines per
+//    CTA (1, 2, 4);
+//  - stencil: output rows per CTA (4, 8, 16) x CTAs per SM of the plane chunks, i.e. the
+//    z-block depth (2, 4, 8).
+// The scratch vectors it writes are overwritten before use by the solve. The stencil
+// shape does not change results; the LU-SGS shape can change the last bits of complex64.
 int MixedBatch::autotune_lusgs(int nact, const int* dlist)
 {
   const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
-  const int cand[3] = {1, 2, 4};
   cudaEvent_t e0, e1;
   CSEM_CUDA_TRY(cudaEventCreate(&e0));
   CSEM_CUDA_TRY(cudaEventCreate(&e1));
-  float best_ms = 1e30f;
-  int best = 0;
-  const bool saved = o32.pipelined_sweeps;
-  o32.pipelined_sweeps = true;
-  for (int vw : cand) {
-    o32.sweep_vw = vw;
-    o32.apply_lusgs(V(0), V(3), nact, dlist, sc);
+  auto time = [&](const std::function<void()>& f) {
+    f();
     CSEM_CUDA_TRY(cudaEventRecord(e0, st));
-    o32.apply_lusgs(V(0), V(3), nact, dlist, sc);
+    f();
     CSEM_CUDA_TRY(cudaEventRecord(e1, st));
     CSEM_CUDA_TRY(cudaEventSynchronize(e1));
     float ms = 0.f;
     CSEM_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = vw;
+    return ms;
+  };
+  const bool saved = o32.pipelined_sweeps, saved_tiled = o32.tiled_sweeps;
+  o32.pipelined_sweeps = true;
+  o32.tiled_sweeps = false;
+  float best_ms = 1e30f;
+  int best_vw = 2, best_lines = 1;
+  for (int vw : {1, 2, 4})
+    for (int lines : {1, 2, 4}) {
+      o32.sweep_vw = vw;
+      o32.sweep_lines = lines;
+      const float ms = time([&]() { o32.apply_lusgs(V(0), V(3), nact, dlist, sc); });
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_vw = vw;
+        best_lines = lines;
+      }
     }
-  }
   o32.pipelined_sweeps = saved;
-  o32.sweep_vw = best;
+  o32.tiled_sweeps = saved_tiled;
+  o32.sweep_vw = best_vw;
+  o32.sweep_lines = best_lines;
+  best_ms = 1e30f;
+  int best_by = 8, best_ctas = 4;
+  for (int by : {4, 8, 16})
+    for (int ctas : {2, 4, 8}) {
+      o32.stencil_by = by;
+      o32.stencil_ctas = ctas;
+      const float ms = time([&]() { o32.apply_A(V(0), V(4), nact, dlist, sc); });
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_by = by;
+        best_ctas = ctas;
+      }
+    }
+  o32.stencil_by = best_by;
+  o32.stencil_ctas = best_ctas;
+  tuned_lines = best_lines;
+  tuned_by = best_by;
+  tuned_ctas = best_ctas;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  return best;
+  return best_vw;
 }
 
 void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions& o, std::vector<MixedResult>& res)

@@ -54,7 +54,8 @@ class MixedBatch {
   // out [nsys][nch][nrec] complex128 from x64
   void extract(int nch, const int* ch, int nrec, const float* rec, double* out_host);
   double inner_seconds = 0, outer_seconds = 0;
-  int tuned_vw = 0;  // sweep width chosen by autotune_lusgs (0: not tuned)
+  int tuned_vw = 0;  // shapes chosen by autotune_lusgs (0: not tuned): sweep width,
+  int tuned_lines = 0, tuned_by = 0, tuned_ctas = 0;  // lines per CTA, stencil rows, stencil CTAs per SM
   long inner_launch_iters = 0;  // sum over launched iterations of active systems
  private:
   void inner_iteration(int nact, const int* dlist, int preco, int maxiter);
@@ -73,7 +74,7 @@ class MixedBatch {
   void run_captured(Graph& g, bool use_graphs, const std::function<void()>& body);
   void drop_gmres_graphs();  // before the GMRES buffers move
   void start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner);
-  int autotune_lusgs(int nact, const int* dlist);  // returns the chosen points per thread
+  int autotune_lusgs(int nact, const int* dlist);  // LU-SGS and stencil shapes; returns the points per thread
   void outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first, const float2* d = nullptr);
   void solve_gmres(const std::vector<double>& bn, const double* tol, const MixedOptions& o,
                    std::vector<MixedResult>& res, std::vector<double>& rnorm, std::vector<int> running);

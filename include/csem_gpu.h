@@ -245,11 +245,16 @@ void *csem_ctx_stream(csem_ctx *c);
  *   "lusgs_tile_rows" rows per warp block of the tiled sweeps: 4, 8 (default) or 16;
  *   "lusgs_tile_vw"   march positions per step of the tiled Ey and Ez sweeps: 1, 2 or 4
  *                     (default);
- *   "autotune"        1: the batched mixed-precision solve times the complex64 LU-SGS
- *                     sweep variants (points per thread 1, 2, 4) on its first running
- *                     systems and keeps the fastest for that batch; 0 (default): the
- *                     fixed default. complex64 results may then differ in the last bits
- *                     from run to run, so it is off by default;
+ *   "autotune"        1: the batched mixed-precision solve times the complex64 kernel
+ *                     shapes on its first running systems and keeps the fastest for that
+ *                     batch: the LU-SGS sweeps' points per thread (1, 2, 4) and lines per
+ *                     CTA (1, 2, 4), the stencil's rows per CTA (4, 8, 16) and plane-chunk
+ *                     depth (CTAs per SM 2, 4, 8); 0 (default): the fixed defaults.
+ *                     complex64 results may then differ in the last bits from run to run,
+ *                     so it is off by default;
+ *   "stencil_by"      stencil tile height, output rows per CTA: 4, 8 (default) or 16;
+ *   "stencil_ctas"    CTAs per SM the stencil's plane chunks aim for (1..16, default 4),
+ *                     which sets the z-block depth. Neither stencil option changes results;
  *   "graphs"          1 (default): the batched BiCGStab replays the iterations between
  *                     two status reads as a captured CUDA graph (from the second time a
  *                     given number of systems is running; not while csem_profile is on);

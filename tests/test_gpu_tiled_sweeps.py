@@ -115,3 +115,27 @@ def test_pipelined_conveyor_of_lines_agrees(gpu, tmp_path, shape):
             assert relerr(got, ref) <= 1e-6, (vw, lines, relerr(got, ref))
     ctx.set_option("lusgs_lines", 1)
     ctx.set_option("lusgs_vw", 0)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{s[1]}x{s[2]}x{s[3]}_air{s[5]}_fvm{s[6]}" for s in SHAPES])
+def test_stencil_shapes_give_identical_bits(gpu, tmp_path, shape):
+    """The stencil's tile height (stencil_by: 4, 8, 16 output rows per CTA) and plane-chunk
+    depth (stencil_ctas) only regroup the same per-point work: complex128 and complex64
+    results are bit-identical for every shape, and complex128 equals the oracle (through
+    the airwave FFT: 1e-12)."""
+    G, ctx, O, _ = _setup(tmp_path, *shape)
+    O.set_freq(0.5)
+    iom = cs.iom_of(0.5)
+    x = probe(ctx.lE, shape[0] + 2)
+    ref64 = ctx.fdfd_apply(iom, x)
+    ref32 = ctx.fdfd_apply(iom, x, c64=True)
+    yo = O.fdfd(x)
+    assert (relerr(ref64, yo) <= 1e-12) if shape[5] else np.array_equal(ref64, yo)
+    for by in (4, 8, 16):
+        for ctas in (1, 4, 16):
+            ctx.set_option("stencil_by", by)
+            ctx.set_option("stencil_ctas", ctas)
+            assert np.array_equal(ctx.fdfd_apply(iom, x), ref64), (by, ctas)
+            assert np.array_equal(ctx.fdfd_apply(iom, x, c64=True), ref32), (by, ctas)
+    ctx.set_option("stencil_by", 8)
+    ctx.set_option("stencil_ctas", 4)
