@@ -28,7 +28,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["k_fdfd.cu", "k_airwave.cu", "k_lusgs.cu", "k_lusgs2.cu", "k_lusgs3.cu", "k_blas.cu", "k_scalar.cu", "k_acq.cu",
+CU_SOURCES = ["k_fdfd.cu", "k_airwave.cu", "k_lusgs.cu", "k_lusgs2.cu", "k_lusgs3.cu", "k_lusgs4.cu", "k_lusgs5.cu", "k_blas.cu", "k_scalar.cu", "k_acq.cu",
               "engine_model.cu", "solve_fp64.cu", "solve_mixed.cu", "prof.cu", "capi.cu", "capi_noalloc.cu",
               "csr_compare.cu"]
 C_SOURCES = ["csem_getpar.c", "csem_setup.c", "csem_partition.c"]

@@ -25,11 +25,13 @@ struct csem_ctx {
   Ops<F32>* ops32 = nullptr;
   Solver64* solver = nullptr;
   MixedBatch* batch = nullptr;
-  DevBuf io[4], sc64, sc32, dotp;
+  DevBuf io[4], sc64, sc32, dotp, groups;
   int nmax64 = 0, nmax32 = 0;
   bool lusgs_pipelined = true;
   int lusgs_vw = 0;
   int lusgs_lines = 1;
+  int lusgs_systems = 1;
+  bool lusgs_split = true;
   int stencil_by = 8, stencil_ctas = 4;
   bool lusgs_tiled = false;
   bool aphi_fix = false;
@@ -45,6 +47,8 @@ template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
   o.pipelined_sweeps = c->lusgs_pipelined;
   o.sweep_vw = c->lusgs_vw;
   o.sweep_lines = c->lusgs_lines;
+  o.sweep_systems = c->lusgs_systems;
+  o.split_sweeps = c->lusgs_split;
   o.stencil_by = c->stencil_by;
   o.stencil_ctas = c->stencil_ctas;
   o.tiled_sweeps = c->lusgs_tiled;
@@ -181,6 +185,11 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
   } else if (!strcmp(name, "lusgs_lines")) {
     if (value < 1 || value > 64) return csem_set_error(CSEM_EINVAL, "lusgs_lines must be in 1..64");
     c->lusgs_lines = value;
+  } else if (!strcmp(name, "lusgs_systems")) {
+    if (value != 1 && value != 2 && value != 4) return csem_set_error(CSEM_EINVAL, "lusgs_systems must be 1, 2 or 4");
+    c->lusgs_systems = value;
+  } else if (!strcmp(name, "lusgs_split")) {
+    c->lusgs_split = value != 0;
   } else if (!strcmp(name, "aphi_fix")) {
     c->aphi_fix = value != 0;
   } else if (!strcmp(name, "lusgs_tiled")) {
@@ -234,8 +243,12 @@ static double batch_bytes(const Model* m, int precision, int preco, int nsys)
     return b;
   };
   if (precision == 32) {
-    // x, b, r, w in complex128; 9 complex64 Krylov vectors; per-system scalars
-    return nsys * (4.0 * 16 * lE + 9.0 * 8 * lE + ops(16) + ops(8) + 4096.0);
+    // x, b, r, w in complex128; 9 complex64 Krylov vectors; per-system scalars; the split
+    // LU-SGS sweeps' (B, w) of the largest component on the sweep grid
+    const double split = preco == PRE_LUSGS
+                             ? 16.0 * (double)sweep_split_scratch(m->n1, m->n2, m->airbc ? m->n3f : m->n3)
+                             : 0.0;
+    return nsys * (4.0 * 16 * lE + 9.0 * 8 * lE + ops(16) + ops(8) + split + 4096.0);
   }
   // the complex128 solver runs one system at a time: 7 BiCGStab vectors or GMRES(m) bases
   return 16.0 * lE * 40 + ops(16);
@@ -736,8 +749,19 @@ static int op_dev(csem_ctx* c, int which, int prec, int nsys, const double* iom,
     Ops<F32>* o = ops32_for(c, nsys);
     const SysScal<F32>* s = c->sc32.as<SysScal<F32>>();
     if (which == OP_A) o->apply_A((const float2*)x, (float2*)y, nsys, nullptr, s);
-    else if (which == OP_LUSGS) o->apply_lusgs((const float2*)x, (float2*)y, nsys, nullptr, s);
-    else o->apply_aphi((const float2*)x, (float2*)y, nsys, nullptr, s);
+    else if (which == OP_LUSGS) {
+      SweepGroups grp;
+      if (o->group_size() > 1) {  // the systems of one frequency, grouped
+        std::vector<int> h;
+        grp.ns = o->group_size();
+        grp.n = build_sweep_groups(nsys, iom, grp.ns, h);
+        ensure(c->groups, sizeof(int) * h.size());
+        // from pageable memory: staged before the call returns, so h may go
+        CSEM_CUDA_TRY(cudaMemcpyAsync(c->groups.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, c->st));
+        grp.dev = c->groups.as<int>();
+      }
+      o->apply_lusgs((const float2*)x, (float2*)y, nsys, nullptr, s, false, &grp);
+    } else o->apply_aphi((const float2*)x, (float2*)y, nsys, nullptr, s);
   }
   CSEM_CUDA_TRY(cudaGetLastError());
   if (user) {

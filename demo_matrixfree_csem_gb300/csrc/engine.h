@@ -70,6 +70,21 @@ bool sweep_pipelined_fits(int comp, int n1, int n2, int nK);  // the sweep's row
 void launch_sweep_tiled(const SweepP<F32>& s, int comp, bool fwd, int nslot, cudaStream_t st, int rows_per_warp,
                         int vw);
 bool sweep_tiled_fits(int comp, int n1, int n2, int nK, int rows_per_warp, int vw);  // the rows fit one CTA
+// complex64 pipelined sweeps with ns systems of one frequency per CTA (k_lusgs4.cu):
+// groups[g * ns + q] is the slot of member q of group g (-1: absent, member 0 present);
+// ns 2 (vw 1 or 2) or 4 (vw 1)
+void launch_sweep_grouped(const SweepP<F32>& s, int comp, bool fwd, const int* groups, int ngroups, int ns, int vw,
+                          cudaStream_t st);
+bool sweep_grouped_fits(int comp, int n1, int n2, int nK);  // at most 256 rows
+// complex64 split sweeps (k_lusgs5.cu): a coalesced pass stores (B, w) of every point in
+// SB (sbs float4 per slot, at least sweep_split_scratch), then the row pipeline runs the
+// chain; vw 1, 2 or 4 points per thread and step. With groups (ns == SPLIT_GROUP: the
+// slots of one frequency, SPLIT_GROUP per group, -1 padded) the pass forms each point's
+// frequency-only coefficients once per group.
+constexpr int SPLIT_GROUP = 16;
+void launch_sweep_split(const SweepP<F32>& s, int comp, bool fwd, int nslot, float4* SB, long sbs, int vw,
+                        const int* groups, int ngroups, int ns, cudaStream_t st);
+long sweep_split_scratch(int n1, int n2, int nK);  // largest component on the sweep grid
 template <class P>
 void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int nslot, cudaStream_t st);
 int sweep_diagonals(int comp, int n1, int n2, int nK);  // number of diagonals t (2..)

@@ -322,8 +322,33 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
   }
 }
 
+int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector<int>& out)
+{
+  out.clear();
+  if (ns < 1) ns = 1;
+  std::vector<char> taken((size_t)nslot, 0);
+  int ng = 0;
+  for (int a = 0; a < nslot; a++) {
+    if (taken[a]) continue;
+    int q = 0;
+    for (int b = a; b < nslot; b++) {
+      if (taken[b] || iom_of_slot[2 * b] != iom_of_slot[2 * a] || iom_of_slot[2 * b + 1] != iom_of_slot[2 * a + 1])
+        continue;
+      if (q == 0) {
+        out.resize(out.size() + ns, -1);
+        ng++;
+      }
+      out[(size_t)(ng - 1) * ns + q] = b;
+      taken[b] = 1;
+      if (++q == ns) q = 0;
+    }
+  }
+  return ng;
+}
+
 template <class P>
-void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, bool bounds_zero)
+void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, bool bounds_zero,
+                         const SweepGroups* grp)
 {
   ProfScope prof(P::exact ? PROF_LUSGS64 : PROF_LUSGS32, st, nslot);
   SweepP<P> s;
@@ -350,6 +375,19 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
     if constexpr (!P::exact) {
       if (tiled_sweeps && sweep_tiled_fits(comp, n1, n2, s.nK, tile_rows, tile_vw)) {
         launch_sweep_tiled(s, comp, fwd, nslot, st, tile_rows, tile_vw);
+        return;
+      }
+      if (split_sweeps && pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
+        const long sbs = sweep_split_scratch(n1, n2, s.nK);
+        if (sb.bytes < sizeof(float4) * (size_t)sbs * nmax) sb.alloc(sizeof(float4) * (size_t)sbs * nmax);
+        const bool g16 = grp && grp->ns == SPLIT_GROUP && grp->n > 0;
+        launch_sweep_split(s, comp, fwd, nslot, sb.as<float4>(), sbs, sweep_vw == 1 || sweep_vw == 4 ? sweep_vw : 2,
+                           g16 ? grp->dev : nullptr, g16 ? grp->n : 0, g16 ? grp->ns : 1, st);
+        return;
+      }
+      if (grp && (grp->ns == 2 || grp->ns == 4) && grp->n > 0 && pipelined_sweeps &&
+          sweep_grouped_fits(comp, n1, n2, s.nK)) {
+        launch_sweep_grouped(s, comp, fwd, grp->dev, grp->n, grp->ns, sweep_vw == 2 && grp->ns == 2 ? 2 : 1, st);
         return;
       }
     }

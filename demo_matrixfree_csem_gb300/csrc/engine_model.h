@@ -73,6 +73,19 @@ class Model {
   template <class P> GridP<P> grid_shifted() const;  // d3/sigma advanced by kstart planes
 };
 
+// Groups of slots at one frequency for the grouped complex64 sweeps (k_lusgs4.cu):
+// dev[g * ns + q] is the slot of member q of group g (-1: absent)
+struct SweepGroups {
+  const int* dev = nullptr;
+  int n = 0;   // groups
+  int ns = 1;  // members per group
+};
+
+// Groups of at most ns slots with equal iom (iom_of_slot[2 slot], [2 slot + 1]), the
+// slots of one frequency in their order, the frequencies in order of first appearance;
+// out gets ngroups * ns entries. Returns the number of groups.
+int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector<int>& out);
+
 // Per-precision workspace for nslot systems on one model.
 template <class P>
 class Ops {
@@ -82,13 +95,22 @@ class Ops {
   Model* m;
   int nmax;
   cudaStream_t st;
-  DevBuf hz0, K, K2, ghx, ghy, cap, V, BV, scal;
+  DevBuf hz0, K, K2, ghx, ghy, cap, V, BV, scal, sb;
   FftPlans* fft;
   // LU-SGS sweeps: true = one pipelined-warp launch per component sweep (k_lusgs2.cu),
   // false = one launch per wavefront diagonal (k_lusgs.cu); both give identical results
   bool pipelined_sweeps = true;
   int sweep_vw = 0;  // points per thread and step of the pipelined sweeps (0: default)
   int sweep_lines = 1;  // complex64: lines one CTA of the pipelined sweeps carries as a conveyor
+  // complex64: systems of one frequency one CTA of the pipelined sweeps carries (1, 2, 4);
+  // used where the caller passes groups of 2 or 4 to apply_lusgs
+  int sweep_systems = 1;
+  // members per group of same-frequency slots the caller should pass to apply_lusgs: 2 or
+  // 4 for the grouped sweeps, SPLIT_GROUP for the split sweeps' pass, 1 for none
+  int group_size() const { return split_sweeps ? SPLIT_GROUP : (sweep_systems >= 4 ? 4 : sweep_systems); }
+  // complex64: each component sweep as a coalesced pass storing every point's (B, w) and a
+  // row pipeline that reads them (k_lusgs5.cu); scratch sb holds the pass's output
+  bool split_sweeps = true;
   int stencil_by = 8;    // stencil tile: output rows per CTA (4, 8, 16)
   int stencil_ctas = 4;  // stencil z-blocks: CTAs per SM the plane chunks aim for
   // complex64 only: line-tiled sweeps (k_lusgs3.cu) instead of the pipelined ones, with
@@ -105,8 +127,9 @@ class Ops {
   // zero (they are never written by the sweeps, so a buffer only ever written by
   // apply_lusgs, or by operations that keep them zero, stays so); then Y is not cleared
   // first. The sweeps overwrite every interior point before reading it.
+  // grp: same-frequency groups of the slots (complex64; sweep_systems > 1 only), or null
   void apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
-                   bool bounds_zero = false);
+                   bool bounds_zero = false, const SweepGroups* grp = nullptr);
   void apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
   void zero(C* Y, long n, int nslot, const int* sys_list);
   ~Ops();

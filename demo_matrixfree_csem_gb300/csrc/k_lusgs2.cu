@@ -33,8 +33,6 @@ using namespace sweep;
 
 namespace {
 
-constexpr int MAXROWS = 512;   // rows of one sweep handled by one CTA (a thread each)
-constexpr int NB_ROWS = 256;   // up to this many rows the warps hand over through named barriers
 // resident CTAs per SM the register budget is sized for, by points per thread and step
 // (complex128 at one point per thread keeps 2, whose 128 registers avoid spilling)
 template <class P, int VW> struct MinBlocks {
@@ -156,104 +154,6 @@ __device__ __forceinline__ typename P::C upd_ez(const SysScal<P>& sc, int fvm, c
   typename P::R vol = fvm ? P::mul(P::mul(X.ds, Y.d), Z.d) : 0;  // Ex's volume (fdfd.c:417)
   return fin<P>(b, aij, geo<P>(X, Y), sg, vol, sc, fvm);
 }
-
-template <class C> __device__ __forceinline__ C shfl_up(C v)
-{
-  C r;
-  r.x = __shfl_up_sync(0xffffffffu, v.x, 1);
-  r.y = __shfl_up_sync(0xffffffffu, v.y, 1);
-  return r;
-}
-
-// Hand-over between warps. Warp w's last row feeds warp w+1's first row one step later
-// through a one-slot buffer in shared memory, synchronised pairwise with named barriers
-// (ids 1 + 2w "full" and 2 + 2w "empty", 64 threads each: the producing and the
-// consuming warp), so a warp waits only for its neighbours, never for the whole CTA.
-// At each step T >= 1 the consumer waits on "full", reads and signals "empty"; at each
-// step the producer (from T >= 1 after waiting on "empty", i.e. once the previous value
-// has been read) writes and signals "full". Each barrier generation therefore holds
-// exactly one producer and one consumer operation, and a final wait on "full" after
-// the loop completes the last one (this protocol was checked exhaustively over warp
-// counts and step counts, under arbitrary interleavings, before use).
-__device__ __forceinline__ void nbar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
-__device__ __forceinline__ void nbar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
-
-// Hand-over state of one CTA. Up to 256 rows (8 warps): the one-slot buffer with the
-// pairwise named barriers described above. Larger CTAs (up to 16 warps; there are only
-// 16 named barriers) use a two-slot buffer and one CTA barrier per step instead.
-template <int VW, class C, bool NAMED> struct HandOff;
-
-template <int VW, class C> struct HandOff<VW, C, true> {
-  C slot[NB_ROWS / 32][VW];
-  // the value the row before this thread's row produced at the previous step: a shuffle
-  // from the previous lane, or the slot for lane 0; the first row reads the zero boundary
-  __device__ __forceinline__ void get(const C (&res)[VW], C (&nb)[VW], int T)
-  {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < VW; q++) nb[q] = shfl_up(res[q]);
-    if (w > 0 && T > 0) {
-      nbar_sync(1 + 2 * (w - 1));  // warp w-1 has written step T-1
-      if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < VW; q++) nb[q] = slot[w - 1][q];
-      }
-      nbar_arrive(2 + 2 * (w - 1));  // the slot may be rewritten
-    } else if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < VW; q++) {
-        nb[q].x = 0;
-        nb[q].y = 0;
-      }
-    }
-  }
-  __device__ __forceinline__ void put(const C (&res)[VW], int T)
-  {
-    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (w + 1 >= nw) return;  // the last warp feeds nobody
-    if (T >= 1) nbar_sync(2 + 2 * w);  // warp w+1 has read step T-1
-    if ((threadIdx.x & 31) == 31) {
-#pragma unroll
-      for (int q = 0; q < VW; q++) slot[w][q] = res[q];
-    }
-    nbar_arrive(1 + 2 * w);
-  }
-  // completes the last generation of the "full" barriers after the step loop
-  __device__ __forceinline__ void finish(int nsteps)
-  {
-    const int w = threadIdx.x >> 5;
-    if (w > 0 && nsteps > 0) nbar_sync(1 + 2 * (w - 1));
-  }
-};
-
-template <int VW, class C> struct HandOff<VW, C, false> {
-  C slot[2][MAXROWS / 32][VW];
-  __device__ __forceinline__ void get(const C (&res)[VW], C (&nb)[VW], int T)
-  {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < VW; q++) nb[q] = shfl_up(res[q]);
-    if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < VW; q++) {
-        C v;
-        v.x = 0;
-        v.y = 0;
-        if (w > 0 && T > 0) v = slot[(T - 1) & 1][w - 1][q];
-        nb[q] = v;
-      }
-    }
-  }
-  __device__ __forceinline__ void put(const C (&res)[VW], int T)
-  {
-    if ((threadIdx.x & 31) == 31) {
-#pragma unroll
-      for (int q = 0; q < VW; q++) slot[T & 1][threadIdx.x >> 5][q] = res[q];
-    }
-    __syncthreads();
-  }
-  __device__ __forceinline__ void finish(int) {}
-};
 
 }  // namespace
 

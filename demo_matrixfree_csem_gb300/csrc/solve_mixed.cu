@@ -129,7 +129,7 @@ void MixedBatch::run_captured(Graph& g, bool use_graphs, const std::function<voi
 void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
 {
   const int* dl = list.as<int>();
-  run_captured(graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter)], o.graphs, [&]() {
+  run_captured(graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter, grp_.n * 8 + grp_.ns)], o.graphs, [&]() {
     for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
   });
 }
@@ -160,7 +160,7 @@ void MixedBatch::inner_iteration(int nact, const int* dl, int preco, int maxiter
   // not cleared before each application
   auto M = [&](const float2* in, float2* out) {
     if (preco == PRE_APHI) o32.apply_aphi(in, out, nact, dl, sc);
-    else o32.apply_lusgs(in, out, nact, dl, sc, true);
+    else o32.apply_lusgs(in, out, nact, dl, sc, true, &grp_);
   };
   M(p, pp);
   o32.apply_A(pp, v, nact, dl, sc);
@@ -174,6 +174,26 @@ void MixedBatch::inner_iteration(int nact, const int* dl, int preco, int maxiter
   launch_xr_dot2<F32>(n, nact, dl, K, d, pp, sh, r, s, t, r0, part, nblk, D + 3 * nsys, D + 4 * nsys, st);
   launch_sc_rs_beta(nact, dl, K, D + 3 * nsys, D + 4 * nsys, nullptr, 0, maxiter, st);
   launch_vec<F32>(VEC_P, n, nact, dl, K, r, p, v, nullptr, nullptr, st);
+}
+
+void MixedBatch::set_list(const std::vector<int>& l)
+{
+  CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, l.data(), sizeof(int) * l.size(), cudaMemcpyHostToDevice, st));
+  grp_ = SweepGroups();
+  const int ns = o32.group_size();
+  if (ns <= 1 || l.empty() || h_iom_.size() < 2 * (size_t)nsys) return;
+  std::vector<double> iom_slot(2 * l.size());
+  for (size_t q = 0; q < l.size(); q++) {
+    iom_slot[2 * q] = h_iom_[2 * (size_t)l[q]];
+    iom_slot[2 * q + 1] = h_iom_[2 * (size_t)l[q] + 1];
+  }
+  const int ng = build_sweep_groups((int)l.size(), iom_slot.data(), ns, grph_);
+  // at most nsys groups of SPLIT_GROUP: allocated once, so the address captured graphs use stays
+  if (!grpbuf.p) grpbuf.alloc(sizeof(int) * SPLIT_GROUP * (size_t)nsys);
+  CSEM_CUDA_TRY(cudaMemcpyAsync(grpbuf.p, grph_.data(), sizeof(int) * grph_.size(), cudaMemcpyHostToDevice, st));
+  grp_.dev = grpbuf.as<int>();
+  grp_.n = ng;
+  grp_.ns = ns;
 }
 
 void MixedBatch::start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner)
@@ -226,14 +246,18 @@ void MixedBatch::outer_update(const std::vector<int>& g, std::vector<double>& rn
 // Autotuner of the complex64 kernel shapes, on the batch's current vectors: each
 // candidate is applied once untimed and once timed with CUDA events on the solver's
 // stream, and the fastest is kept for the rest of this batch.
-//  - LU-SGS: points per thread and step of the pipelined sweeps (1, 2, 4) x lines per
-//    CTA (1, 2, 4);
+//  - LU-SGS: the split sweeps (a coalesced pass and a light row pipeline) at 1, 2, 4
+//    points per thread and step; the one-pass pipelined sweeps at points per thread
+//    (1, 2, 4) x lines per CTA (1, 2, 4), or with 2 (1 or 2 points) or 4 (1 point)
+//    systems of one frequency per CTA;
 //  - stencil: output rows per CTA (4, 8, 16) x CTAs per SM of the plane chunks, i.e. the
 //    z-block depth (2, 4, 8).
 // The scratch vectors it writes are overwritten before use by the solve. The stencil
 // shape does not change results; the LU-SGS shape can change the last bits of complex64.
-int MixedBatch::autotune_lusgs(int nact, const int* dlist)
+int MixedBatch::autotune_lusgs(const std::vector<int>& running)
 {
+  const int nact = (int)running.size();
+  const int* dlist = list.as<int>();
   const SysScal<F32>* sc = sc32.as<SysScal<F32>>();
   cudaEvent_t e0, e1;
   CSEM_CUDA_TRY(cudaEventCreate(&e0));
@@ -252,18 +276,32 @@ int MixedBatch::autotune_lusgs(int nact, const int* dlist)
   o32.pipelined_sweeps = true;
   o32.tiled_sweeps = false;
   float best_ms = 1e30f;
-  int best_vw = 2, best_lines = 1;
-  for (int vw : {1, 2, 4})
-    for (int lines : {1, 2, 4}) {
-      o32.sweep_vw = vw;
-      o32.sweep_lines = lines;
-      const float ms = time([&]() { o32.apply_lusgs(V(0), V(3), nact, dlist, sc); });
-      if (ms < best_ms) {
-        best_ms = ms;
-        best_vw = vw;
-        best_lines = lines;
-      }
+  int best_vw = 2, best_lines = 1, best_ns = 1;
+  bool best_split = true;
+  for (int split : {1, 0})
+    for (int ns : {1, 2, 4}) {
+      if (split && ns > 1) continue;
+      o32.split_sweeps = split != 0;
+      o32.sweep_systems = ns;
+      set_list(running);  // the groups for this candidate (the split pass's, or ns per CTA)
+      for (int vw : {1, 2, 4})
+        for (int lines : {1, 2, 4}) {
+          if ((split && lines > 1) || (ns > 1 && lines > 1) || (ns == 2 && vw == 4) || (ns == 4 && vw > 1)) continue;
+          o32.sweep_vw = vw;
+          o32.sweep_lines = lines;
+          const float ms = time([&]() { o32.apply_lusgs(V(0), V(3), nact, dlist, sc, false, &grp_); });
+          if (ms < best_ms) {
+            best_ms = ms;
+            best_vw = vw;
+            best_lines = lines;
+            best_ns = ns;
+            best_split = split != 0;
+          }
+        }
     }
+  o32.split_sweeps = best_split;
+  o32.sweep_systems = best_ns;
+  set_list(running);
   o32.pipelined_sweeps = saved;
   o32.tiled_sweeps = saved_tiled;
   o32.sweep_vw = best_vw;
@@ -284,6 +322,8 @@ int MixedBatch::autotune_lusgs(int nact, const int* dlist)
   o32.stencil_by = best_by;
   o32.stencil_ctas = best_ctas;
   tuned_lines = best_lines;
+  tuned_systems = best_ns;
+  tuned_split = best_split ? 1 : 0;
   tuned_by = best_by;
   tuned_ctas = best_ctas;
   cudaEventDestroy(e0);
@@ -302,6 +342,7 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
   }
   CSEM_CUDA_TRY(cudaMemcpyAsync(sc64.p, s64.data(), sizeof(SysScal<F64>) * nsys, cudaMemcpyHostToDevice, st));
   CSEM_CUDA_TRY(cudaMemcpyAsync(sc32.p, s32.data(), sizeof(SysScal<F32>) * nsys, cudaMemcpyHostToDevice, st));
+  h_iom_.assign(iom, iom + 2 * (size_t)nsys);
   CSEM_CUDA_TRY(cudaMemsetAsync(x64.p, 0, sizeof(double2) * (size_t)nsys * n, st));
   CSEM_CUDA_TRY(cudaMemcpyAsync(r64.p, b64.p, sizeof(double2) * (size_t)nsys * n, cudaMemcpyDeviceToDevice, st));
   CSEM_CUDA_TRY(cudaMemsetAsync(ks.p, 0, sizeof(KrylovScalars) * nsys, st));
@@ -329,14 +370,13 @@ void MixedBatch::solve(const double* iom, const double* tol, const MixedOptions&
     return;
   }
   if (o.autotune && o.preco != PRE_APHI && !running.empty()) {
-    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, running.data(), sizeof(int) * running.size(), cudaMemcpyHostToDevice, st));
-    tuned_vw = autotune_lusgs((int)running.size(), list.as<int>());
+    tuned_vw = autotune_lusgs(running);
   }
   start_inner(running, ti);
   std::vector<KrylovScalars> kh(nsys);
   inner_launch_iters = 0;
   while (!running.empty()) {
-    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, running.data(), sizeof(int) * running.size(), cudaMemcpyHostToDevice, st));
+    set_list(running);
     inner_iterations((int)running.size(), o);
     inner_launch_iters += (long)running.size() * o.check_every;
     CSEM_CUDA_TRY(cudaGetLastError());
@@ -566,7 +606,7 @@ void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double
   CSEM_CUDA_TRY(cudaMemcpyAsync(st, sh.data(), sizeof(GmState) * nsys, cudaMemcpyHostToDevice, this->st));
   auto M = [&](const float2* in, float2* out, int na, const int* dl) {  // Z_j: only written here
     if (o.preco == PRE_APHI) o32.apply_aphi(in, out, na, dl, sc);
-    else o32.apply_lusgs(in, out, na, dl, sc, true);
+    else o32.apply_lusgs(in, out, na, dl, sc, true, &grp_);
   };
   // r0 = r64 / |r64|, d = 0 (k_start_inner writes r, r0, p, d: here r0 twice and d)
   {
@@ -583,7 +623,7 @@ void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double
     if (act.empty()) break;
     const int na = (int)act.size();
     const unsigned nb32 = (unsigned)((na + 31) / 32);
-    CSEM_CUDA_TRY(cudaMemcpyAsync(list.p, act.data(), sizeof(int) * na, cudaMemcpyHostToDevice, this->st));
+    set_list(act);
     // r = r0 - A d  (d = 0 on the first cycle), v_0 = r / |r|
     if (cycle == 0) {
       CSEM_CUDA_TRY(cudaMemcpyAsync(GW, GR0, sizeof(float2) * N, cudaMemcpyDeviceToDevice, this->st));
@@ -612,7 +652,7 @@ void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double
       dim3 grd((unsigned)((n + 255) / 256), (unsigned)na);
       count_launch(), k_gm_update<<<grd, 256, 0, this->st>>>(n, dl, st, ycoef, nsys, GZ(0), N, GD);
     };
-    run_captured(gm_graphs_[std::make_tuple(na, m, o.preco, 0)], o.graphs, steps);
+    run_captured(gm_graphs_[std::make_tuple(na, m, o.preco, 0, grp_.n * 8 + grp_.ns)], o.graphs, steps);
     CSEM_CUDA_TRY(cudaGetLastError());
     CSEM_CUDA_TRY(cudaMemcpyAsync(sh.data(), st, sizeof(GmState) * nsys, cudaMemcpyDeviceToHost, this->st));
     CSEM_CUDA_TRY(cudaStreamSynchronize(this->st));

@@ -56,6 +56,8 @@ class MixedBatch {
   double inner_seconds = 0, outer_seconds = 0;
   int tuned_vw = 0;  // shapes chosen by autotune_lusgs (0: not tuned): sweep width,
   int tuned_lines = 0, tuned_by = 0, tuned_ctas = 0;  // lines per CTA, stencil rows, stencil CTAs per SM
+  int tuned_systems = 0;  // systems of one frequency per CTA
+  int tuned_split = -1;   // 1: split sweeps chosen
   long inner_launch_iters = 0;  // sum over launched iterations of active systems
  private:
   void inner_iteration(int nact, const int* dlist, int preco, int maxiter);
@@ -68,13 +70,21 @@ class MixedBatch {
     int seen = 0;       // times the combination occurred
     bool failed = false;
   };
-  std::map<std::tuple<int, int, int, int>, Graph> graphs_, gm_graphs_;
+  // keyed by (systems, options..., preconditioner groups): the groups set the sweeps' grids
+  std::map<std::tuple<int, int, int, int, int>, Graph> graphs_, gm_graphs_;
   // body() launched directly the first time g's combination occurs, as a captured CUDA
   // graph from the second time on (never while per-operator profiling records events)
   void run_captured(Graph& g, bool use_graphs, const std::function<void()>& body);
   void drop_gmres_graphs();  // before the GMRES buffers move
   void start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner);
-  int autotune_lusgs(int nact, const int* dlist);  // LU-SGS and stencil shapes; returns the points per thread
+  // the active systems into list and, for grouped complex64 sweeps (o32.sweep_systems >
+  // 1), their same-frequency groups into grp_
+  void set_list(const std::vector<int>& l);
+  std::vector<double> h_iom_;  // iom per system (re, im) of the current solve
+  std::vector<int> grph_;
+  DevBuf grpbuf;
+  SweepGroups grp_;
+  int autotune_lusgs(const std::vector<int>& running);  // LU-SGS and stencil shapes; returns the points per thread
   void outer_update(const std::vector<int>& g, std::vector<double>& rnorm, bool first, const float2* d = nullptr);
   void solve_gmres(const std::vector<double>& bn, const double* tol, const MixedOptions& o,
                    std::vector<MixedResult>& res, std::vector<double>& rnorm, std::vector<int> running);

@@ -37,6 +37,10 @@ def main(argv=None) -> None:
     ap.add_argument("--schedule", choices=["pipelined", "diagonal"], default="pipelined")
     ap.add_argument("--vw", type=int, default=0)
     ap.add_argument("--lines", type=int, default=1, help="lines per CTA of the complex64 pipelined sweeps")
+    ap.add_argument("--systems", type=int, default=1,
+                    help="systems of one frequency per CTA of the complex64 pipelined sweeps (1, 2, 4)")
+    ap.add_argument("--split", type=int, default=0,
+                    help="1: complex64 LU-SGS as a coalesced (B, w) pass and a light row pipeline")
     ap.add_argument("--by", type=int, default=8, help="stencil output rows per CTA")
     ap.add_argument("--ctas", type=int, default=4, help="stencil CTAs per SM of the plane chunks")
     ap.add_argument("--tiled", type=int, default=0, help="1: line-tiled complex64 LU-SGS sweeps")
@@ -68,6 +72,8 @@ def main(argv=None) -> None:
     ctx.set_option("lusgs_pipelined", 1 if a.schedule == "pipelined" else 0)
     ctx.set_option("lusgs_vw", a.vw)
     ctx.set_option("lusgs_lines", a.lines)
+    ctx.set_option("lusgs_systems", a.systems)
+    ctx.set_option("lusgs_split", a.split)
     ctx.set_option("stencil_by", a.by)
     ctx.set_option("stencil_ctas", a.ctas)
     ctx.set_option("lusgs_tiled", a.tiled)
@@ -112,13 +118,15 @@ def main(argv=None) -> None:
         ctx.set_option("lusgs_pipelined", 1)
         ctx.set_option("lusgs_vw", 0)
         ctx.set_option("lusgs_lines", 1)
+        ctx.set_option("lusgs_systems", 1)
+        ctx.set_option("lusgs_split", 0)
         apply()
         torch.cuda.synchronize()
         d = (y1 - y).abs().max().item()
         check = {"max_abs_diff": d, "rel": d / max(y.abs().max().item(), 1e-300),
                  "bit_identical": bool(torch.equal(torch.view_as_real(y1), torch.view_as_real(y)))}
     out = {"workload": a.workload, "op": a.op, "prec": a.prec, "nsys": a.nsys, "schedule": a.schedule,
-           "vw": a.vw, "lines": a.lines, "by": a.by, "ctas": a.ctas, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
+           "vw": a.vw, "lines": a.lines, "systems": a.systems, "split": a.split, "by": a.by, "ctas": a.ctas, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
            "ms_per_application": ms, "ms_per_system": ms / a.nsys,
            "algorithmic_bytes_per_system": per_sys,
            "algorithmic_GBps": per_sys * a.nsys / (ms * 1e-3) / 1e9 if per_sys else None}

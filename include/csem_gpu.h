@@ -225,11 +225,24 @@ void *csem_ctx_stream(csem_ctx *c);
  * options; complex64 results may differ in the last bits between schedules:
  *   "lusgs_pipelined" 1 (default): one launch per LU-SGS component sweep, rows as a
  *                     lockstep pipeline; 0: one launch per wavefront diagonal;
- *   "lusgs_vw"        points per thread and step of the pipelined sweeps: 1, 2, 4, or
- *                     0 for the default (2 complex64, 1 complex128).
- *   "lusgs_lines"     complex64 only: lines one CTA of the pipelined sweeps carries one
- *                     after the other (1..64), so the row pipeline fills and drains once
- *                     per CTA instead of once per line; 1 (default): one line per CTA;
+ *   "lusgs_vw"        points per thread and step of the pipelined (and split) sweeps: 1,
+ *                     2, 4, or 0 for the default (2 complex64, 1 complex128).
+ *   "lusgs_lines"     complex64 with lusgs_split 0 only: lines one CTA of the pipelined
+ *                     sweeps carries one after the other (1..64), so the row pipeline fills
+ *                     and drains once per CTA instead of once per line; 1 (default): one
+ *                     line per CTA;
+ *   "lusgs_split"     complex64 only. 1 (default): each LU-SGS component sweep runs as
+ *                     a coalesced pass that forms every point's b/aii + w (known - cross)
+ *                     and w = iwmu/aii (once per point for all the systems of a frequency)
+ *                     and a row pipeline that reads them and runs only the dependent chain;
+ *                     0: the one-pass pipelined sweeps. Same values to rounding;
+ *   "lusgs_systems"   complex64 only: systems of one frequency one CTA of the pipelined
+ *                     sweeps carries, 1 (default), 2 or 4. The members share the loads of
+ *                     the grid and the frequency-only part of each point's update, and
+ *                     each warp runs one dependent chain per member. With 2, lusgs_vw 2
+ *                     gives 2 points per thread and step, any other value 1; 4 takes 1.
+ *                     Sweeps of more than 256 rows run one system per CTA. Applies with
+ *                     lusgs_split 0;
  *   "lusgs_tiled"     complex64 only. 1: line-tiled sweeps - 32 independent lines per CTA
  *                     (one lane each), the rows cut into one block per warp; 0: the
  *                     schedule chosen by lusgs_pipelined. Same values as the pipelined
@@ -247,8 +260,9 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     (default);
  *   "autotune"        1: the batched mixed-precision solve times the complex64 kernel
  *                     shapes on its first running systems and keeps the fastest for that
- *                     batch: the LU-SGS sweeps' points per thread (1, 2, 4) and lines per
- *                     CTA (1, 2, 4), the stencil's rows per CTA (4, 8, 16) and plane-chunk
+ *                     batch: split or one-pass LU-SGS sweeps, their points per thread
+ *                     (1, 2, 4), lines per CTA (1, 2, 4) and systems per CTA (1, 2, 4), the
+ *                     stencil's rows per CTA (4, 8, 16) and plane-chunk
  *                     depth (CTAs per SM 2, 4, 8); 0 (default): the fixed defaults.
  *                     complex64 results may then differ in the last bits from run to run,
  *                     so it is off by default;

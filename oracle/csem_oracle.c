@@ -78,9 +78,9 @@ orc_ctx_t *orc_create(const orc_desc_t *d)
   c->lHz = (long)n1 * n2 * (n3 + 1);
   c->lH = c->lHx + c->lHy + c->lHz;
   c->lv = (long)(n1 + 1) * (n2 + 1) * (n3 + 1);
-  /* Hy is written up to n1*(n2+1)*n3 past its start; size the buffer for that */
-  long hneed = c->lHx + (long)n1 * (n2 + 1) * n3;
-  if (hneed < c->lH) hneed = c->lH;
+  /* Hy is written up to n1*(n2+1)*n3 past its start; size the buffer for that, and for
+     the corrected Hy length (orc_set_hy_length) */
+  long hneed = c->lHx + (long)n1 * (n2 + 1) * (n3 > n2 ? n3 : n2) + c->lHz;
   c->xh = (double *)calloc(2 * (size_t)hneed, sizeof(double));
   c->v = (double *)calloc(2 * (size_t)c->lv, sizeof(double));
   c->bv = (double *)calloc(2 * (size_t)c->lv, sizeof(double));
@@ -118,6 +118,15 @@ void orc_set_freq(orc_ctx_t *c, float freq)
 void orc_sizes(const orc_ctx_t *c, long *o)
 {
   o[0] = c->lE; o[1] = c->lEx; o[2] = c->lEy; o[3] = c->lEz; o[4] = c->lH; o[5] = c->lv; o[6] = c->n3;
+}
+
+void orc_set_hy_length(orc_ctx_t *c, int sic)
+{
+  /* sic != 0: fdfd.c:59's n1*(n2+1)*n2, so that Hz starts inside Hy when n2 < n3 and the
+     two overlap; sic == 0: n1*(n2+1)*n3, disjoint. Identical whenever n2 == n3, and the
+     overlap is absent whenever n2 >= n3. */
+  c->lHy = (long)c->n1 * (c->n2 + 1) * (sic ? c->n2 : c->n3);
+  c->lH = c->lHx + c->lHy + c->lHz;
 }
 
 void orc_get_h(const orc_ctx_t *c, double *h) { memcpy(h, c->xh, sizeof(double) * 2 * (size_t)c->lH); }

@@ -57,6 +57,9 @@ void orc_sizes(const orc_ctx_t *c, long *out);
 void orc_fdfd_apply(orc_ctx_t *c, const double *x, double *y);
 /* legacy one-pass Dirichlet operator (fdfd.c:212-284), a cross-check of the above */
 void orc_fdfd_apply_old(orc_ctx_t *c, const double *x, double *y);
+/* Hy scratch length: sic != 0 (the default) as fdfd.c:59 (n1*(n2+1)*n2: Hy and Hz overlap
+   when n2 < n3, and fdfd_apply then mixes the two), 0 for n1*(n2+1)*n3. */
+void orc_set_hy_length(orc_ctx_t *c, int sic);
 void orc_get_h(const orc_ctx_t *c, double *h);
 /* y = M^-1 x, LU-SGS (fdfd.c:287-510) */
 void orc_lusgs_apply(orc_ctx_t *c, const double *x, double *y);

@@ -184,6 +184,7 @@ class Oracle:
             L.orc_set_iom.argtypes = [C.c_void_p, C.c_double, C.c_double]
             L.orc_set_freq.argtypes = [C.c_void_p, C.c_float]
             L.orc_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
+            L.orc_set_hy_length.argtypes = [C.c_void_p, C.c_int]
             for nm in ("orc_fdfd_apply", "orc_fdfd_apply_old", "orc_lusgs_apply", "orc_aphi_apply",
                        "orc_get_h"):
                 getattr(L, nm).argtypes = [C.c_void_p, _dp, _dp] if nm != "orc_get_h" else [C.c_void_p, _dp]
@@ -253,6 +254,15 @@ class Oracle:
         y = np.zeros(self.lE, np.complex128)
         fn(self.ctx, _p(x.view(np.float64)), _p(y.view(np.float64)))
         return y
+
+    def set_hy_length(self, sic: bool):
+        """sic=True (default): the reference's Hy length n1*(n2+1)*n2 (fdfd.c:59), which
+        overlaps Hz when n2 < n3; False: n1*(n2+1)*n3."""
+        L = self.lib()
+        L.orc_set_hy_length(self.ctx, int(bool(sic)))
+        s = (C.c_long * 7)()
+        L.orc_sizes(self.ctx, s)
+        self.lH = s[4]
 
     def fdfd(self, x):
         return self._op(self.lib().orc_fdfd_apply, x)

@@ -24,6 +24,11 @@ needs to compare the off-diagonal couplings only:
                  I*omega*mu0 times fdfd_apply's entry there;
       iom        I*omega*mu0 as Acsr_init forms it.
 
+A third fixture pins the reference's Hy scratch length (fdfd.c:59 sizes Hy as
+n1*(n2+1)*n2, where n3 is meant): on a model with n2 < n3 the Hy and Hz scratch overlap
+and fdfd_apply mixes the two. hy_overlap/ holds that model (case.json: its flags) and
+  hy_overlap/fdfd.npz   x, Ax = fdfd_apply(x) and the frequency.
+
 Run where the reference sources exist (CSEM_REFERENCE_DIR, else a sibling directory
 "reference" of this repository):
     python tests/golden/make_known_answers.py
@@ -92,6 +97,31 @@ def run_case(case: str, what: str) -> None:
             os.chdir(cwd)
 
 
+HY_OVERLAP = os.path.join(HERE, "hy_overlap")
+
+
+def run_hy_overlap() -> None:
+    from demo_matrixfree_csem_gb300 import synthetic
+    from oracle import Ref
+    d = HY_OVERLAP
+    cfg = synthetic.random_small(18, nx=6, ny=3, nz=7, nb=2, airbc=0, preco=1, fvm=0)  # n2 = 7 < n3 = 11
+    synthetic.write_config(cfg, d)
+    args = [a.replace(d + "/", "") for a in cfg.args(d)]
+    with open(os.path.join(d, "case.json"), "w") as f:
+        json.dump(args, f, indent=1)
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        R = Ref(args)
+        assert R.n2 < R.n3, (R.n2, R.n3)
+        R.set_freq(0)
+        rng = np.random.default_rng(18)
+        x = (rng.integers(-2 ** 20, 2 ** 20, R.lE) + 1j * rng.integers(-2 ** 20, 2 ** 20, R.lE)) / 2 ** 20
+        np.savez_compressed(os.path.join(d, "fdfd.npz"), x=x, Ax=R.apply(0, x), freq=R.freqs[0])
+    finally:
+        os.chdir(cwd)
+
+
 def main() -> None:
     from oracle import ref_available
     if not ref_available():
@@ -99,6 +129,11 @@ def main() -> None:
     if len(sys.argv) > 2:
         run_case(sys.argv[1], sys.argv[2])
         return
+    if sys.argv[1:] == ["hy_overlap"]:
+        run_hy_overlap()
+        return
+    subprocess.run([sys.executable, __file__, "hy_overlap"], check=True, stdout=subprocess.DEVNULL)
+    print("wrote hy_overlap")
     for case in EXTENDED:
         subprocess.run([sys.executable, __file__, case, "extended"], check=True, stdout=subprocess.DEVNULL)
         print("wrote", case, "extended")

@@ -248,3 +248,27 @@ def test_stencil_couplings_match_reference_assembled_operator(gpu, case):
     lhs = (z["Ax_csr"] - z["self_term"])[m]
     rhs = (complex(z["iom"]) * (y - z["fdfd_diag"] * z["x"]))[m]
     assert relerr(rhs, lhs) <= 1e-13
+
+
+def test_fdfd_keeps_h_disjoint_where_reference_overlaps(gpu):
+    """Where n2 < n3 the reference's Hy scratch (n1*(n2+1)*n2 long, fdfd.c:59) overlaps
+    Hz and its fdfd_apply mixes them (known answer tests/golden/hy_overlap/fdfd.npz). The
+    GPU stencil never stores H, so it computes the curl-curl operator that the reference
+    computes whenever n2 >= n3: bit-identical to the oracle at the disjoint Hy length, and
+    different from the reference's overlapped result."""
+    import json
+    import os
+
+    from cases import GOLDEN
+    d = os.path.join(GOLDEN, "hy_overlap")
+    p = parse_args(json.load(open(os.path.join(d, "case.json"))))
+    z = np.load(os.path.join(d, "fdfd.npz"))
+    G = product_grid(d, p)
+    ctx = cs.Ctx(G, 0, 0)
+    assert ctx.n2 < ctx.n3
+    O = oracle_for(G, p)
+    O.set_hy_length(False)
+    O.set_freq(float(z["freq"]))
+    y = ctx.fdfd_apply(cs.iom_of(float(z["freq"])), z["x"])
+    assert np.array_equal(y, O.fdfd(z["x"]))
+    assert not np.array_equal(y, z["Ax"])

@@ -124,3 +124,40 @@ def test_stencil_couplings_match_reference_assembled_operator(case):
     lhs = (z["Ax_csr"] - z["self_term"])[m]
     rhs = (complex(z["iom"]) * (y - z["fdfd_diag"] * z["x"]))[m]
     assert relerr(rhs, lhs) <= 1e-13
+
+
+def _hy_overlap_case():
+    import json
+    import os
+
+    from cases import GOLDEN
+    d = os.path.join(GOLDEN, "hy_overlap")
+    p = parse_args(json.load(open(os.path.join(d, "case.json"))))
+    return d, p, np.load(os.path.join(d, "fdfd.npz"))
+
+
+def test_oracle_reproduces_reference_hy_overlap():
+    """Known answer (tests/golden/make_known_answers.py): on a model with n2 < n3 the
+    reference's Hy scratch, sized n1*(n2+1)*n2 (fdfd.c:59), overlaps Hz, and its
+    fdfd_apply mixes the two. The oracle at the reference's length reproduces that bit
+    for bit; at the disjoint length n1*(n2+1)*n3 it gives another result, so the overlap
+    is what changes it."""
+    d, p, z = _hy_overlap_case()
+    O = oracle_for(product_grid(d, p), p)
+    assert O.g.n2 < O.n3
+    O.set_freq(float(z["freq"]))
+    assert np.array_equal(O.fdfd(z["x"]), z["Ax"])
+    O.set_hy_length(False)
+    assert not np.array_equal(O.fdfd(z["x"]), z["Ax"])
+
+
+def test_hy_length_is_irrelevant_when_n2_at_least_n3():
+    """The two Hy lengths give the same bits whenever the scratch does not overlap."""
+    d, args, gold = load_golden("lusgs_air0")
+    p = parse_args(args)
+    O = oracle_for(product_grid(d, p), p)
+    assert O.g.n2 >= O.n3
+    O.set_freq(float(gold["freqs"][0]))
+    a = O.fdfd(gold["x"])
+    O.set_hy_length(False)
+    assert np.array_equal(O.fdfd(gold["x"]), a)
