@@ -17,7 +17,8 @@
  *                 (the reference reads it nb rows higher, inject_extract.c:55-63);
  *   dot_order=1   complex128 dot products in the reference's sequential order (its
  *                 iterates bit for bit, slowly);
- *   graphs=0|1, autotune=0|1   the context options of csem_ctx_set_option.
+ *   graphs=0|1, autotune=0|1, lusgs_split, lusgs_vw, lusgs_pipelined, stencil_by,
+ *   stencil_ctas   the context options of csem_ctx_set_option.
  */
 #include <math.h>
 #include <stdarg.h>
@@ -157,8 +158,9 @@ int main(int argc, char **argv)
   csem_ctx *ctx;
   check(csem_ctx_create(&g, airbc, fvm, &ctx));
   {
-    static const char *opt_keys[] = {"fix_quirks", "dot_order", "graphs", "autotune"};
-    for (int q = 0; q < 4; q++) {
+    static const char *opt_keys[] = {"fix_quirks", "dot_order", "graphs", "autotune", "lusgs_split", "lusgs_vw",
+                                     "lusgs_pipelined", "stencil_by", "stencil_ctas"};
+    for (int q = 0; q < (int)(sizeof(opt_keys) / sizeof(opt_keys[0])); q++) {
       int v;
       if (csem_getparint(opt_keys[q], &v)) check(csem_ctx_set_option(ctx, opt_keys[q], v));
     }

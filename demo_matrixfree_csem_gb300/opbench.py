@@ -39,8 +39,9 @@ def main(argv=None) -> None:
     ap.add_argument("--lines", type=int, default=1, help="lines per CTA of the complex64 pipelined sweeps")
     ap.add_argument("--systems", type=int, default=1,
                     help="systems of one frequency per CTA of the complex64 pipelined sweeps (1, 2, 4)")
-    ap.add_argument("--split", type=int, default=0,
-                    help="1: complex64 LU-SGS as a coalesced (B, w) pass and a light row pipeline")
+    ap.add_argument("--split", type=int, default=1,
+                    help="complex64 LU-SGS as a coalesced (B, w) pass and a light row pipeline (1, the "
+                         "default) or one pass (0)")
     ap.add_argument("--by", type=int, default=8, help="stencil output rows per CTA")
     ap.add_argument("--ctas", type=int, default=4, help="stencil CTAs per SM of the plane chunks")
     ap.add_argument("--tiled", type=int, default=0, help="1: line-tiled complex64 LU-SGS sweeps")

@@ -110,15 +110,43 @@ def test_driver_all_sources_writes_one_file_per_source(gpu, tmp_path):
             gf, wf = g_.split(" \t "), w_.split(" \t ")
             assert gf[0] == str(s + 1) and wf[0] == "1" and gf[1:] == wf[1:]
     assert not os.path.exists(all_dir / "emf_0004.txt")
-    mixed = tmp_path / "mixed"
-    mixed.mkdir()
-    for f in os.listdir(tmp_path):
-        if os.path.isfile(tmp_path / f):
-            shutil.copy(tmp_path / f, mixed / f)
-    run(["fsrc=three.txt", "nsrc=all", "precision=32"], mixed)
+
+
+def test_driver_all_sources_mixed_precision_matches_complex128(gpu, tmp_path):
+    """The batched mixed-precision driver (precision=32: every (source, frequency) system
+    in one batch) reports every system converged and writes, per source, the receivers
+    of the complex128 driver to 1e-5 relative. On a 40 x 27 x 19 cell model with three
+    sources and the airwave boundary (airbc=1), the setting of every mixed-precision
+    workload: with airbc=0 the air layers are part of the operator and the complex64
+    inner solves stagnate near a relative residual of 1e-7 (the mixed solver then
+    reports maxiter; measured on this model and on the golden ones)."""
+    from demo_matrixfree_csem_gb300 import build, synthetic
+    cfg = synthetic.random_small(71, nx=40, ny=27, nz=19, nb=4, airbc=1, fvm=0, n1fft=64, n2fft=64)
+    synthetic.write_config(cfg, str(tmp_path))
+    lines = open(tmp_path / "sources.txt").read().splitlines()
+    head, row = lines[0], lines[1].split()
+    srcs = []
+    for s, dx in enumerate((0.0, 150.0, -220.0)):
+        r = list(row)
+        r[0] = "%f" % (float(row[0]) + dx)
+        r[5] = str(s + 1)
+        srcs.append(" ".join(r))
+    (tmp_path / "three.txt").write_text(head + "\n" + "\n".join(srcs) + "\n")
+    base = [a for a in cfg.args(str(tmp_path))[1:] if not a.startswith("fsrc=")]
+    base += [f"fsrc={tmp_path}/three.txt", "nsrc=all", "niter=1000"]
+    out = {}
+    for prec in (64, 32):
+        d = tmp_path / f"p{prec}"
+        d.mkdir()
+        r = subprocess.run([build.DRIVER, *base, f"precision={prec}", "verb=1"], cwd=d, capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        if prec == 32:
+            st = [ln for ln in r.stdout.splitlines() if ln.startswith("source ") and "status" in ln]
+            assert len(st) == 3 * len(cfg.params["freqs"].split(",")), st
+            assert all("status 1," in ln for ln in st), st  # CSEM_ST_CONVERGED
+        out[prec] = [np.array([[float(v) for v in ln.split(" \t ")[4:6]] for ln in
+                               open(d / f"emf_{s + 1:04d}.txt").read().splitlines()[1:]]) for s in range(3)]
     for s in range(3):
-        a = np.array([[float(v) for v in ln.split(" \t ")[4:6]] for ln in
-                      open(all_dir / f"emf_{s + 1:04d}.txt").read().splitlines()[1:]])
-        b = np.array([[float(v) for v in ln.split(" \t ")[4:6]] for ln in
-                      open(mixed / f"emf_{s + 1:04d}.txt").read().splitlines()[1:]])
-        assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
+        a, b = out[64][s], out[32][s]
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max(), (s, np.abs(a - b).max() / np.abs(a).max())
