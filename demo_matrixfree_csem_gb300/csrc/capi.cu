@@ -32,6 +32,8 @@ struct csem_ctx {
   int lusgs_lines = 1;
   int lusgs_systems = 1;
   bool lusgs_split = true;
+  bool lusgs_overlap = true;
+  int lusgs_cap = 0;
   int stencil_by = 8, stencil_ctas = 4;
   bool lusgs_tiled = false;
   bool aphi_fix = false;
@@ -49,6 +51,8 @@ template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
   o.sweep_lines = c->lusgs_lines;
   o.sweep_systems = c->lusgs_systems;
   o.split_sweeps = c->lusgs_split;
+  o.split_overlap = c->lusgs_overlap;
+  o.split_cap = c->lusgs_cap;
   o.stencil_by = c->stencil_by;
   o.stencil_ctas = c->stencil_ctas;
   o.tiled_sweeps = c->lusgs_tiled;
@@ -190,6 +194,11 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     c->lusgs_systems = value;
   } else if (!strcmp(name, "lusgs_split")) {
     c->lusgs_split = value != 0;
+  } else if (!strcmp(name, "lusgs_overlap")) {
+    c->lusgs_overlap = value != 0;
+  } else if (!strcmp(name, "lusgs_cap")) {
+    if (value < 0 || value > 16) return csem_set_error(CSEM_EINVAL, "lusgs_cap must be in 0..16");
+    c->lusgs_cap = value;
   } else if (!strcmp(name, "aphi_fix")) {
     c->aphi_fix = value != 0;
   } else if (!strcmp(name, "lusgs_tiled")) {
@@ -754,7 +763,9 @@ static int op_dev(csem_ctx* c, int which, int prec, int nsys, const double* iom,
       if (o->group_size() > 1) {  // the systems of one frequency, grouped
         std::vector<int> h;
         grp.ns = o->group_size();
-        grp.n = build_sweep_groups(nsys, iom, grp.ns, h);
+        grp.n = grp.ns == SPLIT_GROUP && o->split_overlap
+                    ? build_sweep_groups_halves(nsys, iom, grp.ns, 4, h, &grp.nA, &grp.ngA)
+                    : build_sweep_groups(nsys, iom, grp.ns, h);
         ensure(c->groups, sizeof(int) * h.size());
         // from pageable memory: staged before the call returns, so h may go
         CSEM_CUDA_TRY(cudaMemcpyAsync(c->groups.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, c->st));

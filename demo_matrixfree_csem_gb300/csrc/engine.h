@@ -84,6 +84,14 @@ bool sweep_grouped_fits(int comp, int n1, int n2, int nK);  // at most 256 rows
 constexpr int SPLIT_GROUP = 16;
 void launch_sweep_split(const SweepP<F32>& s, int comp, bool fwd, int nslot, float4* SB, long sbs, int vw,
                         const int* groups, int ngroups, int ns, cudaStream_t st);
+// the two halves of launch_sweep_split; max_ctas > 0 caps the pipeline's grid (each CTA
+// then takes several lines in turn), which leaves room on the SMs for the passes of
+// another stream
+void launch_split_prep(const SweepP<F32>& s, int comp, bool fwd, int nslot, float4* SB, long sbs, const int* groups,
+                       int ngroups, int ns, cudaStream_t st);
+void launch_split_sweep(const SweepP<F32>& s, int comp, bool fwd, int nslot, const float4* SB, long sbs, int vw,
+                        int max_ctas, cudaStream_t st);
+int sm_count();  // multiprocessors of the current device
 long sweep_split_scratch(int n1, int n2, int nK);  // largest component on the sweep grid
 template <class P>
 void launch_sweep(const SweepP<P>& s, int comp, bool fwd, bool aphi, int t, int nslot, cudaStream_t st);

@@ -287,9 +287,21 @@ Ops<P>::Ops(Model* m_, int nslot_max, cudaStream_t st_) : m(m_), nmax(nslot_max)
     CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, cap.bytes, st));  // its boundary planes stay zero
     fft = &m->fft_plans;
   }
+  if (!P::exact) {  // the second stream of the overlapped split sweeps (created outside any capture)
+    CSEM_CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+    CSEM_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CSEM_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  }
 }
 
-template <class P> Ops<P>::~Ops() {}
+template <class P> Ops<P>::~Ops()
+{
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (aux) cudaStreamDestroy(aux);
+}
+
+template <class P> int Ops<P>::split_ctas() const { return split_cap > 0 ? split_cap * sm_count() : 0; }
 
 template <class P>
 void Ops<P>::zero(C* Y, long n, int nslot, const int* sys_list)
@@ -346,6 +358,21 @@ int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector
   return ng;
 }
 
+int build_sweep_groups_halves(int nslot, const double* iom_of_slot, int ns, int min_half, std::vector<int>& out,
+                              int* nA, int* ngA)
+{
+  *nA = *ngA = 0;
+  if (min_half < 1 || nslot < 2 * min_half) return build_sweep_groups(nslot, iom_of_slot, ns, out);
+  const int a = nslot / 2;
+  std::vector<int> g2;
+  const int na = build_sweep_groups(a, iom_of_slot, ns, out);
+  const int nb = build_sweep_groups(nslot - a, iom_of_slot + 2 * (size_t)a, ns, g2);
+  out.insert(out.end(), g2.begin(), g2.end());
+  *nA = a;
+  *ngA = na;
+  return na + nb;
+}
+
 template <class P>
 void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, bool bounds_zero,
                          const SweepGroups* grp)
@@ -369,6 +396,49 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
     if (!bounds_zero) CSEM_CUDA_TRY(cudaMemsetAsync(cap.p, 0, sizeof(C) * (size_t)s.capE * nslot, st));
   }
   if (!bounds_zero) zero(Y, m->lE, nslot, sys_list);
+  if constexpr (!P::exact) {
+    // split sweeps on two halves of the slots, one per stream, the second starting once the
+    // first half's first pass is queued: a half's passes (HBM-bound) then run while the
+    // other half's pipelines (hand-over-bound) do
+    const bool all_fit = sweep_pipelined_fits(0, n1, n2, s.nK) && sweep_pipelined_fits(1, n1, n2, s.nK) &&
+                         sweep_pipelined_fits(2, n1, n2, s.nK);
+    if (split_sweeps && split_overlap && pipelined_sweeps && !tiled_sweeps && all_fit && aux && grp &&
+        grp->ns == SPLIT_GROUP && grp->nA > 0 && grp->nA < nslot && grp->ngA > 0 && grp->ngA < grp->n) {
+      const long sbs = sweep_split_scratch(n1, n2, s.nK);
+      if (sb.bytes < sizeof(float4) * (size_t)sbs * nmax) sb.alloc(sizeof(float4) * (size_t)sbs * nmax);
+      const int nA = grp->nA, nB = nslot - nA, vw = sweep_vw == 1 || sweep_vw == 4 ? sweep_vw : 2;
+      SweepP<P> sB = s;
+      if (s.sys_list) {
+        sB.sys_list = s.sys_list + nA;
+      } else {  // slot = system: the second half's systems start nA systems in
+        sB.X = s.X + (size_t)nA * m->lE;
+        sB.Y = s.Y + (size_t)nA * m->lE;
+        sB.scal = s.scal + nA;
+      }
+      if (s.CAP) sB.CAP = s.CAP + (size_t)nA * s.capE;
+      float4* SA = sb.as<float4>();
+      float4* SBh = SA + (size_t)nA * sbs;
+      const int* gA = grp->dev;
+      const int* gB = grp->dev + (size_t)grp->ngA * grp->ns;
+      const int cap = split_ctas();
+      static const int order[6][2] = {{0, 1}, {1, 1}, {2, 1}, {2, 0}, {1, 0}, {0, 0}};
+      for (int q = 0; q < 6; q++) {
+        const int comp = order[q][0];
+        const bool fwd = order[q][1] != 0;
+        launch_split_prep(s, comp, fwd, nA, SA, sbs, gA, grp->ngA, grp->ns, st);
+        if (q == 0) {
+          CSEM_CUDA_TRY(cudaEventRecord(ev_fork, st));
+          CSEM_CUDA_TRY(cudaStreamWaitEvent(aux, ev_fork, 0));
+        }
+        launch_split_sweep(s, comp, fwd, nA, SA, sbs, vw, cap, st);
+        launch_split_prep(sB, comp, fwd, nB, SBh, sbs, gB, grp->n - grp->ngA, grp->ns, aux);
+        launch_split_sweep(sB, comp, fwd, nB, SBh, sbs, vw, cap, aux);
+      }
+      CSEM_CUDA_TRY(cudaEventRecord(ev_join, aux));
+      CSEM_CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
+      return;
+    }
+  }
   // both schedules visit the points of a sweep in an order that respects every
   // dependency of the lexicographic sweep, so they may be mixed sweep by sweep
   auto sweep = [&](int comp, bool fwd) {

@@ -79,12 +79,21 @@ struct SweepGroups {
   const int* dev = nullptr;
   int n = 0;   // groups
   int ns = 1;  // members per group
+  // split sweeps run as two halves on two streams when nA > 0: slots [0, nA) and
+  // [nA, nslot); the first ngA groups hold slots of the first half, the others slots of
+  // the second, each numbered from the start of its half
+  int nA = 0, ngA = 0;
 };
 
 // Groups of at most ns slots with equal iom (iom_of_slot[2 slot], [2 slot + 1]), the
 // slots of one frequency in their order, the frequencies in order of first appearance;
 // out gets ngroups * ns entries. Returns the number of groups.
 int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector<int>& out);
+// The same for the two halves of the slots when nslot >= 2 * min_half (*nA = nslot / 2,
+// *ngA the first half's groups, slot numbers local to each half); otherwise one set and
+// *nA = *ngA = 0. Returns the number of groups.
+int build_sweep_groups_halves(int nslot, const double* iom_of_slot, int ns, int min_half, std::vector<int>& out,
+                              int* nA, int* ngA);
 
 // Per-precision workspace for nslot systems on one model.
 template <class P>
@@ -111,6 +120,13 @@ class Ops {
   // complex64: each component sweep as a coalesced pass storing every point's (B, w) and a
   // row pipeline that reads them (k_lusgs5.cu); scratch sb holds the pass's output
   bool split_sweeps = true;
+  // split sweeps on two halves of the slots, one on `aux`, so that one half's passes can
+  // run while the other half's pipelines do; split_cap > 0 runs the pipelines as that many
+  // CTAs per SM, each taking lines in turn (0: one CTA per line)
+  bool split_overlap = true;
+  int split_cap = 0;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int stencil_by = 8;    // stencil tile: output rows per CTA (4, 8, 16)
   int stencil_ctas = 4;  // stencil z-blocks: CTAs per SM the plane chunks aim for
   // complex64 only: line-tiled sweeps (k_lusgs3.cu) instead of the pipelined ones, with
@@ -132,6 +148,7 @@ class Ops {
                    bool bounds_zero = false, const SweepGroups* grp = nullptr);
   void apply_aphi(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
   void zero(C* Y, long n, int nslot, const int* sys_list);
+  int split_ctas() const;  // the split pipelines' grid cap on two streams: split_cap CTAs per SM (0: none)
   ~Ops();
 };
 

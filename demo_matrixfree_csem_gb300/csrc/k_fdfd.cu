@@ -233,6 +233,19 @@ __global__ void k_hz0(GridP<P> g, const SysScal<P>* __restrict__ scal, const typ
   out[(size_t)slot * g.n1 * g.n2 + i + (long)g.n1 * j] = hz;
 }
 
+int sm_count()
+{
+  static int sms[64] = {};  // per device, queried once
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    sms[dev] = 152;
+  }
+  return sms[dev];
+}
+
 // by: output rows per CTA (4, 8 or 16; other values: 8); ctas_per_sm: how many CTAs per
 // SM the grid aims for when it splits the planes into chunks (other than 1..16: 4), which
 // sets the z-block depth. Neither changes any result: every output takes the same
@@ -246,15 +259,7 @@ static void launch_fdfd_by(const GridP<P>& g, const SysScal<P>* scal, const type
   const int gx = (g.n1 + 1 + 30) / 31, gy = (g.n2 + 1 + BY - 1) / BY;
   const long base = (long)gx * gy * nsys;
   // split the planes into chunks until about ctas_per_sm CTAs per SM are in the grid
-  static int sms[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-    (void)cudaGetLastError();
-    sms[dev] = 152;
-  }
-  int nkc = (int)(((long)ctas_per_sm * sms[dev] + base - 1) / base);
+  int nkc = (int)(((long)ctas_per_sm * sm_count() + base - 1) / base);
   const int maxc = (g.n3 + 1) / 8 > 0 ? (g.n3 + 1) / 8 : 1;  // chunks of at least 8 planes
   if (nkc > maxc) nkc = maxc;
   if (nkc < 1) nkc = 1;

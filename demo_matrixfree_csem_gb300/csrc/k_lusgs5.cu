@@ -171,13 +171,18 @@ template <int VW, int NW> struct SplitBounds {
 
 }  // namespace
 
-// Ex: rows k, march j, VW consecutive i per thread. grid (i groups, slots)
+// Ex: rows k, march j, VW consecutive i per thread; a line is an i group of one slot
 template <bool FWD, int VW, int NW>
-__global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_ex32s(SweepP<F32> s, const float4* SB, long sbs)
+__global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_ex32s(SweepP<F32> s, const float4* SB, long sbs, int nslot)
 {
   typedef float2 C;
   __shared__ typename HandSel<VW, NW>::type hand;
-  const int slot = blockIdx.y;
+  // a CTA takes lines (i group, slot) in turn: one per CTA when the grid covers them all,
+  // several when the grid is capped (each line's hand-over generations balance, so the
+  // next line starts on the same barriers)
+  const int nlines = (s.g.n1 + VW - 1) / VW;
+  for (long item = blockIdx.x; item < (long)nlines * nslot; item += gridDim.x) {
+  const int slot = (int)(item / nlines);
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<F32>& g = s.g;
   const int n1 = g.n1, n2 = g.n2, nK = s.nK;
@@ -187,7 +192,7 @@ __global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_ex32s(SweepP<F32> s, const f
   const int rr = threadIdx.x;
   const bool rowok = rr < R_;
   const int k = FWD ? 1 + rr : R_ - rr;
-  const int i0 = blockIdx.x * VW;
+  const int i0 = (int)(item % nlines) * VW;
   float gn = 0.f;
   C* ex0 = nullptr;
   const float4* sb = nullptr;
@@ -250,22 +255,30 @@ __global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_ex32s(SweepP<F32> s, const f
     if (nxt) make();
   }
   hand.finish(M + R_ - 1);
+  // every warp has closed this line's barrier generations before any starts the next:
+  // a producer's first put of the next line does not wait on "empty", and a second
+  // arrival on "full" before its consumer's last sync would complete that generation
+  // without the consumer (checked by simulating the protocol over 1-8 warps, 1-6 steps
+  // and 1-4 lines per CTA under random interleavings: it deadlocks without this barrier)
+  __syncthreads();
+  }
 }
 
-// Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j): march i in chunks of VW.
-// grid (lines, slots)
+// Ey (COMP 1: line j, rows k) / Ez (COMP 2: line k, rows j): march i in chunks of VW
 template <int COMP, bool FWD, int VW, int NW>
-__global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_eyz32s(SweepP<F32> s, const float4* SB, long sbs)
+__global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_eyz32s(SweepP<F32> s, const float4* SB, long sbs, int nslot)
 {
   typedef float2 C;
   __shared__ typename HandSel<VW, NW>::type hand;
-  const int slot = blockIdx.y;
+  const int nlines = COMP == 1 ? s.g.n2 : s.nK;  // lines (j for Ey, k for Ez) x slots, in turn as in k_sweep_ex32s
+  for (long item = blockIdx.x; item < (long)nlines * nslot; item += gridDim.x) {
+  const int slot = (int)(item / nlines);
   const int sys = s.sys_list ? s.sys_list[slot] : slot;
   const GridP<F32>& g = s.g;
   const int n1 = g.n1, n2 = g.n2, nK = s.nK;
   const View<F32> V = view_of<F32>(s, slot, sys);
   const C z = make_float2(0.f, 0.f);
-  const int line = blockIdx.x;
+  const int line = (int)(item % nlines);
   const int R_ = COMP == 1 ? nK - 1 : n2 - 1;  // rows k (Ey) or j (Ez) = 1..R_
   const int M = n1 - 1;                         // march i = 1..M
   const int NC = (M + VW - 1) / VW;
@@ -343,6 +356,8 @@ __global__ void CSEM_SWEEP_BOUNDS_S(VW, NW) k_sweep_eyz32s(SweepP<F32> s, const 
     if (nx) make(c + 1);
   }
   hand.finish(NC + R_ - 1);
+  __syncthreads();  // close this line's barrier generations first (see k_sweep_ex32s)
+  }
 }
 
 long sweep_split_scratch(int n1, int n2, int nK)
@@ -354,41 +369,41 @@ long sweep_split_scratch(int n1, int n2, int nK)
 
 template <int VW, int NW>
 static void launch_split_nw(const SweepP<F32>& s, int comp, bool fwd, int nslot, const float4* SB, long sbs,
-                            cudaStream_t st)
+                            int max_ctas, cudaStream_t st)
 {
   const int n1 = s.g.n1, n2 = s.g.n2, nK = s.nK;
   const int rows = comp == 2 ? n2 - 1 : nK - 1;
   const int threads = NW ? NW * 32 : (rows + 31) / 32 * 32;
+  const long nlines = comp == 0 ? (n1 + VW - 1) / VW : (comp == 1 ? n2 : nK);
+  long items = nlines * nslot;
+  const unsigned grd = (unsigned)(max_ctas > 0 && items > max_ctas ? max_ctas : items);
   if (comp == 0) {
-    dim3 grd((n1 + VW - 1) / VW, nslot);
-    if (fwd) count_launch(), k_sweep_ex32s<true, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs);
-    else count_launch(), k_sweep_ex32s<false, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs);
+    if (fwd) count_launch(), k_sweep_ex32s<true, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs, nslot);
+    else count_launch(), k_sweep_ex32s<false, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs, nslot);
   } else if (comp == 1) {
-    dim3 grd(n2, nslot);
-    if (fwd) count_launch(), k_sweep_eyz32s<1, true, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs);
-    else count_launch(), k_sweep_eyz32s<1, false, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs);
+    if (fwd) count_launch(), k_sweep_eyz32s<1, true, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs, nslot);
+    else count_launch(), k_sweep_eyz32s<1, false, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs, nslot);
   } else {
-    dim3 grd(nK, nslot);
-    if (fwd) count_launch(), k_sweep_eyz32s<2, true, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs);
-    else count_launch(), k_sweep_eyz32s<2, false, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs);
+    if (fwd) count_launch(), k_sweep_eyz32s<2, true, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs, nslot);
+    else count_launch(), k_sweep_eyz32s<2, false, VW, NW><<<grd, threads, 0, st>>>(s, SB, sbs, nslot);
   }
 }
 
 template <int VW>
 static void launch_split_vw(const SweepP<F32>& s, int comp, bool fwd, int nslot, const float4* SB, long sbs,
-                            cudaStream_t st)
+                            int max_ctas, cudaStream_t st)
 {
   const int rows = comp == 2 ? s.g.n2 - 1 : s.nK - 1;
   switch ((rows + 31) / 32) {  // warps of the CTA: one row per thread
-    case 1: launch_split_nw<VW, 1>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 2: launch_split_nw<VW, 2>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 3: launch_split_nw<VW, 3>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 4: launch_split_nw<VW, 4>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 5: launch_split_nw<VW, 5>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 6: launch_split_nw<VW, 6>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 7: launch_split_nw<VW, 7>(s, comp, fwd, nslot, SB, sbs, st); break;
-    case 8: launch_split_nw<VW, 8>(s, comp, fwd, nslot, SB, sbs, st); break;
-    default: launch_split_nw<VW < 4 ? VW : 2, 0>(s, comp, fwd, nslot, SB, sbs, st); break;  // 257..512 rows
+    case 1: launch_split_nw<VW, 1>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 2: launch_split_nw<VW, 2>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 3: launch_split_nw<VW, 3>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 4: launch_split_nw<VW, 4>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 5: launch_split_nw<VW, 5>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 6: launch_split_nw<VW, 6>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 7: launch_split_nw<VW, 7>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    case 8: launch_split_nw<VW, 8>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;
+    default: launch_split_nw<VW < 4 ? VW : 2, 0>(s, comp, fwd, nslot, SB, sbs, max_ctas, st); break;  // 257..512 rows
   }
 }
 
@@ -407,8 +422,8 @@ static void launch_prep(const SweepP<F32>& s, int nslot, float4* SB, long sbs, c
   }
 }
 
-void launch_sweep_split(const SweepP<F32>& s, int comp, bool fwd, int nslot, float4* SB, long sbs, int vw,
-                        const int* groups, int ngroups, int ns, cudaStream_t st)
+void launch_split_prep(const SweepP<F32>& s, int comp, bool fwd, int nslot, float4* SB, long sbs, const int* groups,
+                       int ngroups, int ns, cudaStream_t st)
 {
   if (comp == 0) {
     if (fwd) launch_prep<0, true>(s, nslot, SB, sbs, groups, ngroups, ns, st);
@@ -420,9 +435,21 @@ void launch_sweep_split(const SweepP<F32>& s, int comp, bool fwd, int nslot, flo
     if (fwd) launch_prep<2, true>(s, nslot, SB, sbs, groups, ngroups, ns, st);
     else launch_prep<2, false>(s, nslot, SB, sbs, groups, ngroups, ns, st);
   }
-  if (vw == 1) launch_split_vw<1>(s, comp, fwd, nslot, SB, sbs, st);
-  else if (vw == 4) launch_split_vw<4>(s, comp, fwd, nslot, SB, sbs, st);
-  else launch_split_vw<2>(s, comp, fwd, nslot, SB, sbs, st);
+}
+
+void launch_split_sweep(const SweepP<F32>& s, int comp, bool fwd, int nslot, const float4* SB, long sbs, int vw,
+                        int max_ctas, cudaStream_t st)
+{
+  if (vw == 1) launch_split_vw<1>(s, comp, fwd, nslot, SB, sbs, max_ctas, st);
+  else if (vw == 4) launch_split_vw<4>(s, comp, fwd, nslot, SB, sbs, max_ctas, st);
+  else launch_split_vw<2>(s, comp, fwd, nslot, SB, sbs, max_ctas, st);
+}
+
+void launch_sweep_split(const SweepP<F32>& s, int comp, bool fwd, int nslot, float4* SB, long sbs, int vw,
+                        const int* groups, int ngroups, int ns, cudaStream_t st)
+{
+  launch_split_prep(s, comp, fwd, nslot, SB, sbs, groups, ngroups, ns, st);
+  launch_split_sweep(s, comp, fwd, nslot, SB, sbs, vw, 0, st);  // one CTA per line
 }
 
 }  // namespace csem

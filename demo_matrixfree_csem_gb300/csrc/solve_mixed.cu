@@ -129,7 +129,8 @@ void MixedBatch::run_captured(Graph& g, bool use_graphs, const std::function<voi
 void MixedBatch::inner_iterations(int nact, const MixedOptions& o)
 {
   const int* dl = list.as<int>();
-  run_captured(graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter, grp_.n * 8 + grp_.ns)], o.graphs, [&]() {
+  run_captured(graphs_[std::make_tuple(nact, o.preco, o.check_every, o.niter, grp_.n * 32 + grp_.ns, grp_.nA, grp_.ngA)],
+               o.graphs, [&]() {
     for (int q = 0; q < o.check_every; q++) inner_iteration(nact, dl, o.preco, o.niter);
   });
 }
@@ -187,13 +188,18 @@ void MixedBatch::set_list(const std::vector<int>& l)
     iom_slot[2 * q] = h_iom_[2 * (size_t)l[q]];
     iom_slot[2 * q + 1] = h_iom_[2 * (size_t)l[q] + 1];
   }
-  const int ng = build_sweep_groups((int)l.size(), iom_slot.data(), ns, grph_);
+  int nA = 0, ngA = 0;
+  const int ng = ns == SPLIT_GROUP && o32.split_overlap
+                     ? build_sweep_groups_halves((int)l.size(), iom_slot.data(), ns, 4, grph_, &nA, &ngA)
+                     : build_sweep_groups((int)l.size(), iom_slot.data(), ns, grph_);
   // at most nsys groups of SPLIT_GROUP: allocated once, so the address captured graphs use stays
   if (!grpbuf.p) grpbuf.alloc(sizeof(int) * SPLIT_GROUP * (size_t)nsys);
   CSEM_CUDA_TRY(cudaMemcpyAsync(grpbuf.p, grph_.data(), sizeof(int) * grph_.size(), cudaMemcpyHostToDevice, st));
   grp_.dev = grpbuf.as<int>();
   grp_.n = ng;
   grp_.ns = ns;
+  grp_.nA = nA;
+  grp_.ngA = ngA;
 }
 
 void MixedBatch::start_inner(const std::vector<int>& g, const std::vector<double>& tol_inner)
@@ -652,7 +658,8 @@ void MixedBatch::gmres_inner(const std::vector<int>& g, const std::vector<double
       dim3 grd((unsigned)((n + 255) / 256), (unsigned)na);
       count_launch(), k_gm_update<<<grd, 256, 0, this->st>>>(n, dl, st, ycoef, nsys, GZ(0), N, GD);
     };
-    run_captured(gm_graphs_[std::make_tuple(na, m, o.preco, 0, grp_.n * 8 + grp_.ns)], o.graphs, steps);
+    run_captured(gm_graphs_[std::make_tuple(na, m, o.preco, 0, grp_.n * 32 + grp_.ns, grp_.nA, grp_.ngA)], o.graphs,
+                 steps);
     CSEM_CUDA_TRY(cudaGetLastError());
     CSEM_CUDA_TRY(cudaMemcpyAsync(sh.data(), st, sizeof(GmState) * nsys, cudaMemcpyDeviceToHost, this->st));
     CSEM_CUDA_TRY(cudaStreamSynchronize(this->st));

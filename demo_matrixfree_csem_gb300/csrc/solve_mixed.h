@@ -71,7 +71,7 @@ class MixedBatch {
     bool failed = false;
   };
   // keyed by (systems, options..., preconditioner groups): the groups set the sweeps' grids
-  std::map<std::tuple<int, int, int, int, int>, Graph> graphs_, gm_graphs_;
+  std::map<std::tuple<int, int, int, int, int, int, int>, Graph> graphs_, gm_graphs_;
   // body() launched directly the first time g's combination occurs, as a captured CUDA
   // graph from the second time on (never while per-operator profiling records events)
   void run_captured(Graph& g, bool use_graphs, const std::function<void()>& body);

@@ -42,6 +42,8 @@ def main(argv=None) -> None:
     ap.add_argument("--split", type=int, default=1,
                     help="complex64 LU-SGS as a coalesced (B, w) pass and a light row pipeline (1, the "
                          "default) or one pass (0)")
+    ap.add_argument("--overlap", type=int, default=1, help="split sweeps on two streams (1, the default) or one (0)")
+    ap.add_argument("--cap", type=int, default=0, help="CTAs per SM of the split pipelines on two streams (0: none)")
     ap.add_argument("--by", type=int, default=8, help="stencil output rows per CTA")
     ap.add_argument("--ctas", type=int, default=4, help="stencil CTAs per SM of the plane chunks")
     ap.add_argument("--tiled", type=int, default=0, help="1: line-tiled complex64 LU-SGS sweeps")
@@ -75,6 +77,8 @@ def main(argv=None) -> None:
     ctx.set_option("lusgs_lines", a.lines)
     ctx.set_option("lusgs_systems", a.systems)
     ctx.set_option("lusgs_split", a.split)
+    ctx.set_option("lusgs_overlap", a.overlap)
+    ctx.set_option("lusgs_cap", a.cap)
     ctx.set_option("stencil_by", a.by)
     ctx.set_option("stencil_ctas", a.ctas)
     ctx.set_option("lusgs_tiled", a.tiled)
@@ -127,7 +131,7 @@ def main(argv=None) -> None:
         check = {"max_abs_diff": d, "rel": d / max(y.abs().max().item(), 1e-300),
                  "bit_identical": bool(torch.equal(torch.view_as_real(y1), torch.view_as_real(y)))}
     out = {"workload": a.workload, "op": a.op, "prec": a.prec, "nsys": a.nsys, "schedule": a.schedule,
-           "vw": a.vw, "lines": a.lines, "systems": a.systems, "split": a.split, "by": a.by, "ctas": a.ctas, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
+           "vw": a.vw, "lines": a.lines, "systems": a.systems, "split": a.split, "overlap": a.overlap, "cap": a.cap, "by": a.by, "ctas": a.ctas, "tiled": a.tiled, "tile_rows": a.tile_rows, "tile_vw": a.tile_vw, "check": check,
            "ms_per_application": ms, "ms_per_system": ms / a.nsys,
            "algorithmic_bytes_per_system": per_sys,
            "algorithmic_GBps": per_sys * a.nsys / (ms * 1e-3) / 1e9 if per_sys else None}

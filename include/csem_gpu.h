@@ -236,6 +236,12 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     and w = iwmu/aii (once per point for all the systems of a frequency)
  *                     and a row pipeline that reads them and runs only the dependent chain;
  *                     0: the one-pass pipelined sweeps. Same values to rounding;
+ *   "lusgs_overlap"   with lusgs_split 1: 1 (default) runs batches of 8 or more systems
+ *                     as two halves on two streams, so that one half's passes overlap the
+ *                     other half's pipelines; 0: one stream. Same bits either way;
+ *   "lusgs_cap"       on two streams, the split pipelines run this many CTAs per SM,
+ *                     each taking lines in turn, to leave the other half's passes room on
+ *                     the SMs (1..16); 0 (default): one CTA per line. Same bits either way;
  *   "lusgs_systems"   complex64 only: systems of one frequency one CTA of the pipelined
  *                     sweeps carries, 1 (default), 2 or 4. The members share the loads of
  *                     the grid and the frequency-only part of each point's update, and

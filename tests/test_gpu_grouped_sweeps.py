@@ -137,3 +137,43 @@ def test_split_sweeps_in_the_mixed_solve(gpu, tmp_path):
     ctx.set_option("lusgs_split", 1)
     for q in range(len(freqs)):
         assert relerr(out[1]["dcal"][q], out[0]["dcal"][q]) <= 1e-6, q
+
+
+@pytest.mark.parametrize("shape", [SHAPES[0], SHAPES[1], SHAPES[2]],
+                         ids=[f"{s[1]}x{s[2]}x{s[3]}_air{s[5]}_fvm{s[6]}" for s in SHAPES[:3]])
+def test_split_sweeps_on_two_streams_give_the_same_bits(gpu, tmp_path, shape):
+    """With 8 or more systems the split sweeps run as two halves of the slots on two
+    streams (lusgs_overlap, the default): each half's passes and pipelines are the same
+    kernels on disjoint systems, so every system gets exactly the bits of the single-stream
+    schedule. 9 systems at mixed frequencies: halves of 4 and 5, each with its own groups.
+    The pipelines on two streams run a capped grid (lusgs_cap CTAs per SM) whose CTAs take
+    lines in turn: with a cap of 1 the CTAs here take one to three lines each."""
+    cfg, G, ctx, O = _setup(tmp_path, *shape)
+    freqs = FREQS + [0.5, 1.0]
+    X = np.stack([probe(ctx.lE, shape[0] + 30 + q) for q in range(len(freqs))])
+    ctx.set_option("lusgs_overlap", 0)
+    one = _lusgs_batch(ctx, freqs, X)
+    ctx.set_option("lusgs_overlap", 1)
+    for cap in (4, 1, 0):
+        ctx.set_option("lusgs_cap", cap)
+        two = _lusgs_batch(ctx, freqs, X)
+        assert np.array_equal(one, two), cap
+    ctx.set_option("lusgs_cap", 4)
+    O.set_freq(freqs[3])
+    assert relerr(two[3], O.lusgs(X[3])) <= 2e-5
+
+
+def test_split_sweeps_on_two_streams_in_the_mixed_solve(gpu, tmp_path):
+    """The batched mixed-precision solve of 10 systems (halves of 5 while all run) gives the
+    same receivers, bit for bit, with one or two streams."""
+    cfg, G, ctx, O = _setup(tmp_path, *SHAPES[1])
+    freqs = np.array([0.5, 0.75, 1.0, 0.5, 0.75, 1.0, 0.5, 0.75, 1.0, 0.5], np.float32)
+    src = np.repeat(cfg.acq.src[:1, :3], len(freqs), axis=0)
+    src[:, 0] += np.arange(len(freqs), dtype=np.float32) * 29.0
+    out = {}
+    for ov in (0, 1):
+        ctx.set_option("lusgs_overlap", ov)
+        out[ov] = cs.solve_batch(ctx, freqs, src, rec=cfg.acq.rec, precision=32, preco=1, niter=1000, tol=1e-8)
+        assert out[ov]["status"] == ["converged"] * len(freqs), (ov, out[ov]["status"])
+    assert np.array_equal(out[0]["dcal"], out[1]["dcal"])
+    assert np.array_equal(out[0]["iters"], out[1]["iters"])
