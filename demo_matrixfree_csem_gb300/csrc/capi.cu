@@ -33,6 +33,7 @@ struct csem_ctx {
   int lusgs_systems = 1;
   bool lusgs_split = true;
   bool lusgs_overlap = true;
+  bool fused_dots = true;
   int lusgs_cap = 0;
   int stencil_by = 8, stencil_ctas = 4;
   bool lusgs_tiled = false;
@@ -52,6 +53,7 @@ template <class P> static void configure(const csem_ctx* c, Ops<P>& o)
   o.sweep_systems = c->lusgs_systems;
   o.split_sweeps = c->lusgs_split;
   o.split_overlap = c->lusgs_overlap;
+  o.fused_dots = c->fused_dots;
   o.split_cap = c->lusgs_cap;
   o.stencil_by = c->stencil_by;
   o.stencil_ctas = c->stencil_ctas;
@@ -194,6 +196,8 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     c->lusgs_systems = value;
   } else if (!strcmp(name, "lusgs_split")) {
     c->lusgs_split = value != 0;
+  } else if (!strcmp(name, "fused_dots")) {
+    c->fused_dots = value != 0;
   } else if (!strcmp(name, "lusgs_overlap")) {
     c->lusgs_overlap = value != 0;
   } else if (!strcmp(name, "lusgs_cap")) {

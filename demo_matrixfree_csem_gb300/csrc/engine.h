@@ -11,6 +11,13 @@ template <class P>
 void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
                  const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
                  cudaStream_t st, int by = 8, int ctas_per_sm = 4);
+// complex64 y = A x with the Krylov dot products of y folded in (k_fdfd EPI): kind 1 sums
+// y conj(E), kind 2 e conj(y) and y conj(y); part gets fdfd_partials(...) partials per slot
+// (kind 2: two sets of nsys), for launch_dot_finish
+void launch_fdfd_dot(const GridP<F32>& g, const SysScal<F32>* scal, const float2* X, float2* Y, const float2* ghx,
+                     const float2* ghy, int nsys, const int* sys_list, cudaStream_t st, int by, int ctas_per_sm,
+                     int kind, const float2* E, double2* part);
+int fdfd_partials(int n1, int n2, int n3, int nsys, int by, int ctas_per_sm);  // CTAs per system of the stencil
 template <class P>
 void launch_hz0(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* out,
                 int nsys, const int* sys_list, cudaStream_t st);
@@ -119,5 +126,8 @@ void launch_dot2(const typename P::C* a1, const typename P::C* b1, const typenam
 // cdotprod.c), into out[0]; one CTA, a dependent chain of n additions
 void launch_dot_seq(const double2* a, const double2* b, long n, double2* out, cudaStream_t st);
 int dot_blocks(long n);
+// out1[slot] (and out2[slot]) = fixed-order sums of partial[slot][0..nblk) (and of
+// partial[nslot + slot][...]), as launch_dot / launch_dot2 finish
+void launch_dot_finish(const double2* partial, int nblk, int nslot, double2* out1, double2* out2, cudaStream_t st);
 
 }  // namespace csem

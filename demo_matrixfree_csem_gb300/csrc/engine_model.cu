@@ -311,27 +311,41 @@ void Ops<P>::zero(C* Y, long n, int nslot, const int* sys_list)
 }
 
 template <class P>
-void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc)
+void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, const DotEpi<P>* epi)
 {
   ProfScope whole(P::exact ? PROF_A64 : PROF_A32, st, nslot);
   const GridP<P>& g = m->grid<P>();
+  const C* ghxp = nullptr;
+  const C* ghyp = nullptr;
   if (m->airbc) {
     const AirP<P>& a = m->air<P>();
-    {
-      ProfScope air(P::exact ? PROF_AIR64 : PROF_AIR32, st, nslot);
-      launch_hz0<P>(g, sc, X, hz0.as<C>(), nslot, sys_list, st);
-      launch_air_gather<P>(a, hz0.as<C>(), K.as<C>(), nslot, st);
-      fft->exec(P::exact, K.p, nslot, CUFFT_FORWARD, st);
-      launch_air_filter<P>(a, K.as<C>(), K2.as<C>(), nslot, st);
-      fft->exec(P::exact, K2.p, 2 * nslot, CUFFT_INVERSE, st);
-      launch_air_scatter<P>(a, K2.as<C>(), ghx.as<C>(), ghy.as<C>(), nslot, st);
-    }
-    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
-    launch_fdfd<P>(g, sc, X, Y, ghx.as<C>(), ghy.as<C>(), nslot, sys_list, st, stencil_by, stencil_ctas);
-  } else {
-    ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
-    launch_fdfd<P>(g, sc, X, Y, nullptr, nullptr, nslot, sys_list, st, stencil_by, stencil_ctas);
+    ProfScope air(P::exact ? PROF_AIR64 : PROF_AIR32, st, nslot);
+    launch_hz0<P>(g, sc, X, hz0.as<C>(), nslot, sys_list, st);
+    launch_air_gather<P>(a, hz0.as<C>(), K.as<C>(), nslot, st);
+    fft->exec(P::exact, K.p, nslot, CUFFT_FORWARD, st);
+    launch_air_filter<P>(a, K.as<C>(), K2.as<C>(), nslot, st);
+    fft->exec(P::exact, K2.p, 2 * nslot, CUFFT_INVERSE, st);
+    launch_air_scatter<P>(a, K2.as<C>(), ghx.as<C>(), ghy.as<C>(), nslot, st);
+    ghxp = ghx.as<C>();
+    ghyp = ghy.as<C>();
   }
+  ProfScope sten(P::exact ? PROF_STENCIL64 : PROF_STENCIL32, st, nslot);
+  if constexpr (!P::exact) {
+    // the dot products folded into the stencil where its partials fit the caller's buffer
+    if (epi && epi->kind && fused_dots &&
+        fdfd_partials(g.n1, g.n2, g.n3, nslot, stencil_by, stencil_ctas) <= epi->cap) {
+      const int np = fdfd_partials(g.n1, g.n2, g.n3, nslot, stencil_by, stencil_ctas);
+      launch_fdfd_dot(g, sc, X, Y, ghxp, ghyp, nslot, sys_list, st, stencil_by, stencil_ctas, epi->kind, epi->e,
+                      epi->partial);
+      launch_dot_finish(epi->partial, np, nslot, epi->out1, epi->kind == 2 ? epi->out2 : nullptr, st);
+      return;
+    }
+  }
+  launch_fdfd<P>(g, sc, X, Y, ghxp, ghyp, nslot, sys_list, st, stencil_by, stencil_ctas);
+  if (epi && epi->kind == 1)
+    launch_dot<P>(Y, epi->e, epi->n, epi->n, nslot, sys_list, epi->partial, epi->nblk, epi->out1, st);
+  else if (epi && epi->kind == 2)
+    launch_dot2<P>(epi->e, Y, Y, Y, epi->n, epi->n, nslot, sys_list, epi->partial, epi->nblk, epi->out1, epi->out2, st);
 }
 
 int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector<int>& out)

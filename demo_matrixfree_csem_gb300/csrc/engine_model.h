@@ -95,6 +95,20 @@ int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector
 int build_sweep_groups_halves(int nslot, const double* iom_of_slot, int ns, int min_half, std::vector<int>& out,
                               int* nA, int* ngA);
 
+// Krylov dot products of A's result y to form with it: kind 1 out1 = <y, e>, kind 2
+// out1 = <e, y> and out2 = <y, y> (<a, b> = sum a conj(b)), per slot; partial holds
+// 2 * nslot * cap doubles2 (cap >= nblk, the blocks of the separate dot products over n)
+template <class P> struct DotEpi {
+  int kind = 0;
+  const typename P::C* e = nullptr;
+  double2* partial = nullptr;
+  int cap = 0;
+  double2* out1 = nullptr;
+  double2* out2 = nullptr;
+  long n = 0;
+  int nblk = 0;
+};
+
 // Per-precision workspace for nslot systems on one model.
 template <class P>
 class Ops {
@@ -137,8 +151,12 @@ class Ops {
   bool aphi_fix = false;
   int tile_rows = 8;
   int tile_vw = 4;
-  // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal)
-  void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc);
+  // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal); with epi,
+  // also the dot products epi asks for: inside the complex64 stencil (fused_dots) where its
+  // partials fit, by the separate dot-product kernels otherwise
+  void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
+               const DotEpi<P>* epi = nullptr);
+  bool fused_dots = true;
   // bounds_zero: the caller guarantees that Y's entries outside the swept interior are
   // zero (they are never written by the sweeps, so a buffer only ever written by
   // apply_lusgs, or by operations that keep them zero, stays so); then Y is not cleared

@@ -10,6 +10,7 @@
 #include "csem_cuda.cuh"
 #include "engine.h"
 #include "solver_state.h"
+#include "k_dot_common.cuh"
 
 namespace csem {
 
@@ -23,46 +24,10 @@ int dot_blocks(long n)
   return (int)b;
 }
 
-struct Acc2 {  // compensated float accumulator for one real component
-  float hi, lo;
-  __device__ __forceinline__ void add(float x)
-  {
-    float s = hi + x;
-    float bb = s - hi;
-    float err = (hi - (s - bb)) + (x - bb);
-    hi = s;
-    lo += err;
-  }
-  __device__ __forceinline__ void addprod(float a, float b)
-  {
-    float p = a * b;
-    float e = fmaf(a, b, -p);
-    add(p);
-    lo += e;
-  }
-  __device__ __forceinline__ void subprod(float a, float b)
-  {
-    float p = a * b;
-    float e = fmaf(a, b, -p);
-    add(-p);
-    lo -= e;
-  }
-  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-
 // a per-system double2 scalar in the vector's precision
 template <class P> __device__ __forceinline__ typename P::C cast_c(double2 v);
 template <> __device__ __forceinline__ double2 cast_c<F64>(double2 v) { return v; }
 template <> __device__ __forceinline__ float2 cast_c<F32>(double2 v) { return make_float2((float)v.x, (float)v.y); }
-
-__device__ __forceinline__ double2 warp_sum(double2 v)
-{
-  for (int o = 16; o > 0; o >>= 1) {
-    v.x = __dadd_rn(v.x, __shfl_down_sync(0xffffffffu, v.x, o));
-    v.y = __dadd_rn(v.y, __shfl_down_sync(0xffffffffu, v.y, o));
-  }
-  return v;
-}
 
 __device__ __forceinline__ double2 block_sum(double2 v)
 {
@@ -78,31 +43,6 @@ __device__ __forceinline__ double2 block_sum(double2 v)
   __syncthreads();
   return v;
 }
-
-// One thread's share of sum a*conj(b) over [beg, end) with stride DOT_THREADS.
-template <class P> struct DotAcc;
-template <> struct DotAcc<F64> {
-  double2 acc = make_double2(0, 0);
-  __device__ __forceinline__ void add(double2 a, double2 b)
-  {
-    double2 x = make_double2(a.x, a.y), y = make_double2(b.x, -b.y);
-    double2 pr = cmul<F64>(x, y);
-    acc.x = __dadd_rn(acc.x, pr.x);
-    acc.y = __dadd_rn(acc.y, pr.y);
-  }
-  __device__ __forceinline__ double2 value() const { return acc; }
-};
-template <> struct DotAcc<F32> {
-  Acc2 re = {0.f, 0.f}, im = {0.f, 0.f};
-  __device__ __forceinline__ void add(float2 a, float2 b)
-  {
-    re.addprod(a.x, b.x);
-    re.addprod(a.y, b.y);
-    im.addprod(a.y, b.x);
-    im.subprod(a.x, b.y);
-  }
-  __device__ __forceinline__ double2 value() const { return make_double2(re.value(), im.value()); }
-};
 
 // partial[slot][blk] = sum over the block's chunk of a*conj(b)
 template <class P>
@@ -296,10 +236,18 @@ void launch_dot2(const typename P::C* a1, const typename P::C* b1, const typenam
   count_launch(), k_dot2_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out1, out2);
 }
 
+void launch_dot_finish(const double2* partial, int nblk, int nslot, double2* out1, double2* out2, cudaStream_t st)
+{
+  if (out2) count_launch(), k_dot2_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out1, out2);
+  else count_launch(), k_dot_final<<<nslot, DOT_THREADS, 0, st>>>(partial, nblk, out1);
+}
+
 template void launch_dot<F64>(const double2*, const double2*, long, long, int, const int*, double2*, int,
                               double2*, cudaStream_t);
 template void launch_dot<F32>(const float2*, const float2*, long, long, int, const int*, double2*, int,
                               double2*, cudaStream_t);
+template void launch_dot2<F64>(const double2*, const double2*, const double2*, const double2*, long, long, int,
+                               const int*, double2*, int, double2*, double2*, cudaStream_t);
 template void launch_dot2<F32>(const float2*, const float2*, const float2*, const float2*, long, long, int,
                                const int*, double2*, int, double2*, double2*, cudaStream_t);
 template void launch_xr_dot2<F32>(long, int, const int*, const KrylovScalars*, float2*, const float2*,

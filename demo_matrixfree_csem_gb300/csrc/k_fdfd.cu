@@ -12,6 +12,7 @@
 // (fdfd.c:151-172); k_hz0 provides that Hz plane.
 #include "csem_cuda.cuh"
 #include "engine.h"
+#include "k_dot_common.cuh"
 
 namespace csem {
 
@@ -52,15 +53,25 @@ __device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __r
 // plane stride per plane; the plane's spacings are uniform loads. H is evaluated exactly
 // as in h_at, so complex128 results keep their bits.
 // resident CTAs per SM the complex64 stencil's register budget is sized for (a build may
-// set CSEM_FDFD_MINB to try others)
+// set CSEM_FDFD_MINB to try others); 544-thread CTAs (BY = 16) get one, i.e. no cap below
+// the 255 registers a thread may hold, as three of them would leave 32 per thread
 #ifndef CSEM_FDFD_MINB
 #define CSEM_FDFD_MINB 3
 #endif
-template <class P, int BY>
-__global__ void __launch_bounds__(32 * (BY + 1), P::exact ? 1 : CSEM_FDFD_MINB)
+//
+// EPI > 0 (complex64) folds the Krylov dot products of the result into the pass: EPI 1
+// sums y conj(e) (BiCGStab's v.r0 after v = A p), EPI 2 sums e conj(y) and y conj(y) (s.t
+// and t.t after t = A s), e read at the outputs' own indices. Each thread accumulates as
+// the dot-product kernels do (compensated float pairs), the CTA sums its threads in a
+// fixed tree and order, and writes part[slot][cta] (EPI 2: and part[nslot + slot][cta]),
+// which launch_dot_finish adds up in a fixed order: deterministic, but a different
+// partition of the sum than launch_dot's.
+template <class P, int BY, int EPI>
+__global__ void __launch_bounds__(32 * (BY + 1), P::exact || BY >= 16 ? 1 : CSEM_FDFD_MINB)
 k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
        typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
-       const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list)
+       const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list,
+       const typename P::C* __restrict__ E, double2* __restrict__ part)
 {
   typedef typename P::C C;
   typedef typename P::R R;
@@ -77,6 +88,18 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
   C* bx = Y + (size_t)sys * g.lE;
   C* by = bx + g.lEx;
   C* bz = by + g.lEy;
+  const C* epx = EPI ? E + (size_t)sys * g.lE : nullptr;  // the dot products' other vector
+  const C* epy = EPI ? epx + g.lEx : nullptr;
+  const C* epz = EPI ? epy + g.lEy : nullptr;
+  DotAcc<P> dacc1, dacc2;
+  auto dot = [&](C y, const C* e, long o) {
+    if constexpr (EPI == 1) {
+      dacc1.add(y, e[o]);
+    } else if constexpr (EPI == 2) {
+      dacc1.add(e[o], y);
+      dacc2.add(y, y);
+    }
+  };
   const C iwmu = scal[sys].iwmu, iom = scal[sys].iom;
   const C* ghx = GHX ? GHX + (size_t)slot * (n1 + 1) * n2 : nullptr;  // ghosts are per slot
   const C* ghy = GHY ? GHY + (size_t)slot * n1 * (n2 + 1) : nullptr;
@@ -186,6 +209,7 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1s, d2), d3), iom));
         }
         bx[oEx] = r;
+        if (EPI) dot(r, epx, oEx);
       }
       if (outY) {  // by
         C r = z;
@@ -197,6 +221,7 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1, d2s), d3), iom));
         }
         by[oEy] = r;
+        if (EPI) dot(r, epy, oEy);
       }
       if (outZ && kin) {  // bz
         C r = z;
@@ -207,12 +232,36 @@ k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __r
           if (g.fvm) r = cmul<P>(r, rmul<P>(P::mul(P::mul(d1, d2), d3s), iom));
         }
         bz[oEz] = r;
+        if (EPI) dot(r, epz, oEz);
       }
     }
     pHx = hx;
     pHy = hy;
     exk = ex1;
     eyk = ey1;
+  }
+  if constexpr (EPI > 0) {
+    __shared__ double2 red[2][BY + 1];
+    const double2 v1 = warp_sum(dacc1.value());
+    const double2 v2 = EPI == 2 ? warp_sum(dacc2.value()) : make_double2(0, 0);
+    if (lane == 0) {
+      red[0][w] = v1;
+      red[1][w] = v2;
+    }
+    __syncthreads();
+    if (w == 0 && lane == 0) {
+      double2 a1 = make_double2(0, 0), a2 = make_double2(0, 0);
+      for (int q = 0; q <= BY; q++) {
+        a1.x = __dadd_rn(a1.x, red[0][q].x);
+        a1.y = __dadd_rn(a1.y, red[0][q].y);
+        a2.x = __dadd_rn(a2.x, red[1][q].x);
+        a2.y = __dadd_rn(a2.y, red[1][q].y);
+      }
+      const int npart = gridDim.x * gridDim.y * nkc, nslot = gridDim.z / nkc;
+      const int cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * kc);
+      part[(size_t)slot * npart + cta] = a1;
+      if (EPI == 2) part[(size_t)(nslot + slot) * npart + cta] = a2;
+    }
   }
 }
 
@@ -250,23 +299,52 @@ int sm_count()
 // SM the grid aims for when it splits the planes into chunks (other than 1..16: 4), which
 // sets the z-block depth. Neither changes any result: every output takes the same
 // operands in the same operations.
-template <class P, int BY>
-static void launch_fdfd_by(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
-                           const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
-                           cudaStream_t st, int ctas_per_sm)
+struct FdfdShape {
+  int gx, gy, nkc, kchunk;
+};
+static FdfdShape fdfd_shape(int n1, int n2, int n3, int nsys, int by, int ctas_per_sm)
 {
-  dim3 blk(32, BY + 1);
-  const int gx = (g.n1 + 1 + 30) / 31, gy = (g.n2 + 1 + BY - 1) / BY;
-  const long base = (long)gx * gy * nsys;
+  if (by != 4 && by != 16) by = 8;
+  if (ctas_per_sm < 1 || ctas_per_sm > 16) ctas_per_sm = 4;
+  FdfdShape f;
+  f.gx = (n1 + 1 + 30) / 31;
+  f.gy = (n2 + 1 + by - 1) / by;
+  const long base = (long)f.gx * f.gy * nsys;
   // split the planes into chunks until about ctas_per_sm CTAs per SM are in the grid
   int nkc = (int)(((long)ctas_per_sm * sm_count() + base - 1) / base);
-  const int maxc = (g.n3 + 1) / 8 > 0 ? (g.n3 + 1) / 8 : 1;  // chunks of at least 8 planes
+  const int maxc = (n3 + 1) / 8 > 0 ? (n3 + 1) / 8 : 1;  // chunks of at least 8 planes
   if (nkc > maxc) nkc = maxc;
   if (nkc < 1) nkc = 1;
-  const int kchunk = (g.n3 + 1 + nkc - 1) / nkc;
-  nkc = (g.n3 + 1 + kchunk - 1) / kchunk;
-  dim3 grd(gx, gy, nsys * nkc);
-  count_launch(), k_fdfd<P, BY><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, kchunk, nkc, sys_list);
+  f.kchunk = (n3 + 1 + nkc - 1) / nkc;
+  f.nkc = (n3 + 1 + f.kchunk - 1) / f.kchunk;
+  return f;
+}
+
+int fdfd_partials(int n1, int n2, int n3, int nsys, int by, int ctas_per_sm)
+{
+  const FdfdShape f = fdfd_shape(n1, n2, n3, nsys, by, ctas_per_sm);
+  return f.gx * f.gy * f.nkc;
+}
+
+template <class P, int BY, int EPI>
+static void launch_fdfd_by(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
+                           const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
+                           cudaStream_t st, int ctas_per_sm, const typename P::C* E, double2* part)
+{
+  const FdfdShape f = fdfd_shape(g.n1, g.n2, g.n3, nsys, BY, ctas_per_sm);
+  dim3 blk(32, BY + 1);
+  dim3 grd(f.gx, f.gy, nsys * f.nkc);
+  count_launch(), k_fdfd<P, BY, EPI><<<grd, blk, 0, st>>>(g, scal, X, Y, ghx, ghy, f.kchunk, f.nkc, sys_list, E, part);
+}
+
+template <class P, int EPI>
+static void launch_fdfd_epi(const GridP<P>& g, const SysScal<P>* scal, const typename P::C* X, typename P::C* Y,
+                            const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
+                            cudaStream_t st, int by, int ctas_per_sm, const typename P::C* E, double2* part)
+{
+  if (by == 4) launch_fdfd_by<P, 4, EPI>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm, E, part);
+  else if (by == 16) launch_fdfd_by<P, 16, EPI>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm, E, part);
+  else launch_fdfd_by<P, 8, EPI>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm, E, part);
 }
 
 template <class P>
@@ -274,10 +352,15 @@ void launch_fdfd(const GridP<P>& g, const SysScal<P>* scal, const typename P::C*
                  const typename P::C* ghx, const typename P::C* ghy, int nsys, const int* sys_list,
                  cudaStream_t st, int by, int ctas_per_sm)
 {
-  if (ctas_per_sm < 1 || ctas_per_sm > 16) ctas_per_sm = 4;
-  if (by == 4) launch_fdfd_by<P, 4>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm);
-  else if (by == 16) launch_fdfd_by<P, 16>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm);
-  else launch_fdfd_by<P, 8>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, ctas_per_sm);
+  launch_fdfd_epi<P, 0>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, by, ctas_per_sm, nullptr, nullptr);
+}
+
+void launch_fdfd_dot(const GridP<F32>& g, const SysScal<F32>* scal, const float2* X, float2* Y, const float2* ghx,
+                     const float2* ghy, int nsys, const int* sys_list, cudaStream_t st, int by, int ctas_per_sm,
+                     int kind, const float2* E, double2* part)
+{
+  if (kind == 2) launch_fdfd_epi<F32, 2>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, by, ctas_per_sm, E, part);
+  else launch_fdfd_epi<F32, 1>(g, scal, X, Y, ghx, ghy, nsys, sys_list, st, by, ctas_per_sm, E, part);
 }
 
 template <class P>
