@@ -33,7 +33,7 @@ struct csem_ctx {
   int lusgs_systems = 1;
   bool lusgs_split = true;
   bool lusgs_overlap = true;
-  bool fused_dots = true;
+  bool fused_dots = false;
   int lusgs_cap = 0;
   int stencil_by = 8, stencil_ctas = 4;
   bool lusgs_tiled = false;

@@ -152,11 +152,12 @@ class Ops {
   int tile_rows = 8;
   int tile_vw = 4;
   // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal); with epi,
-  // also the dot products epi asks for: inside the complex64 stencil (fused_dots) where its
-  // partials fit, by the separate dot-product kernels otherwise
+  // also the dot products epi asks for: inside the complex64 stencil where fused_dots is on
+  // and its partials fit, by the separate dot-product kernels otherwise (the default: they
+  // measured faster)
   void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
                const DotEpi<P>* epi = nullptr);
-  bool fused_dots = true;
+  bool fused_dots = false;
   // bounds_zero: the caller guarantees that Y's entries outside the swept interior are
   // zero (they are never written by the sweeps, so a buffer only ever written by
   // apply_lusgs, or by operations that keep them zero, stays so); then Y is not cleared

@@ -236,10 +236,11 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     and w = iwmu/aii (once per point for all the systems of a frequency)
  *                     and a row pipeline that reads them and runs only the dependent chain;
  *                     0: the one-pass pipelined sweeps. Same values to rounding;
- *   "fused_dots"      1 (default): the batched complex64 BiCGStab forms v.r0 after v = A p
- *                     and s.t, t.t after t = A s inside the operator's stencil (one
- *                     deterministic partial per CTA); 0: separate dot-product passes. The
- *                     two partition the sums differently (results differ in rounding);
+ *   "fused_dots"      1: the batched complex64 BiCGStab forms v.r0 after v = A p and s.t,
+ *                     t.t after t = A s inside the operator's stencil (one deterministic
+ *                     partial per CTA); 0 (default): separate dot-product passes, which
+ *                     measured faster (the compensated sums double the stencil's
+ *                     instructions). The two partition the sums differently;
  *   "lusgs_overlap"   with lusgs_split 1: 1 (default) runs batches of 8 or more systems
  *                     as two halves on two streams, so that one half's passes overlap the
  *                     other half's pipelines; 0: one stream. Same bits either way;

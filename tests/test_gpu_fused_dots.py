@@ -1,4 +1,4 @@
-"""The BiCGStab dot products folded into the complex64 stencil (fused_dots, the default):
+"""The BiCGStab dot products folded into the complex64 stencil (fused_dots=1, an option):
 after v = A p the stencil also sums v.r0, after t = A s it sums s.t and t.t, each CTA
 writing one deterministic partial that the dot products' fixed-order final reduction adds
 up. Through the batched mixed-precision solve (C ABI):
@@ -49,7 +49,7 @@ def test_fused_dots_remove_two_launches_per_iteration(gpu, model):
         b, nb = _solve(cfg, ctx, 1, niter=8, check_every=8)
     finally:
         ctx.set_option("graphs", 1)
-        ctx.set_option("fused_dots", 1)
+        ctx.set_option("fused_dots", 0)
     assert na - nb == 2 * 8, (na, nb)
 
 
@@ -58,6 +58,7 @@ def test_fused_dots_converge_to_the_same_receivers(gpu, model):
     sep, _ = _solve(cfg, ctx, 0)
     fus, _ = _solve(cfg, ctx, 1)
     again, _ = _solve(cfg, ctx, 1)
+    ctx.set_option("fused_dots", 0)
     assert sep["status"] == ["converged"] * 6 and fus["status"] == ["converged"] * 6
     for q in range(6):
         assert relerr(fus["dcal"][q], sep["dcal"][q]) <= 1e-6, q
