@@ -311,7 +311,7 @@ void Ops<P>::zero(C* Y, long n, int nslot, const int* sys_list)
 }
 
 template <class P>
-void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, const DotEpi<P>* epi)
+bool Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc, const DotEpi<P>* epi)
 {
   ProfScope whole(P::exact ? PROF_A64 : PROF_A32, st, nslot);
   const GridP<P>& g = m->grid<P>();
@@ -338,14 +338,11 @@ void Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
       launch_fdfd_dot(g, sc, X, Y, ghxp, ghyp, nslot, sys_list, st, stencil_by, stencil_ctas, epi->kind, epi->e,
                       epi->partial);
       launch_dot_finish(epi->partial, np, nslot, epi->out1, epi->kind == 2 ? epi->out2 : nullptr, st);
-      return;
+      return true;
     }
   }
   launch_fdfd<P>(g, sc, X, Y, ghxp, ghyp, nslot, sys_list, st, stencil_by, stencil_ctas);
-  if (epi && epi->kind == 1)
-    launch_dot<P>(Y, epi->e, epi->n, epi->n, nslot, sys_list, epi->partial, epi->nblk, epi->out1, st);
-  else if (epi && epi->kind == 2)
-    launch_dot2<P>(epi->e, Y, Y, Y, epi->n, epi->n, nslot, sys_list, epi->partial, epi->nblk, epi->out1, epi->out2, st);
+  return false;
 }
 
 int build_sweep_groups(int nslot, const double* iom_of_slot, int ns, std::vector<int>& out)

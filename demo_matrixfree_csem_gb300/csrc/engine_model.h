@@ -151,11 +151,11 @@ class Ops {
   bool aphi_fix = false;
   int tile_rows = 8;
   int tile_vw = 4;
-  // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal); with epi,
-  // also the dot products epi asks for: inside the complex64 stencil where fused_dots is on
-  // and its partials fit, by the separate dot-product kernels otherwise (the default: they
-  // measured faster)
-  void apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
+  // y = A x for nslot slots (sys_list maps slot -> system index in X/Y/scal). With epi,
+  // the complex64 stencil also forms the dot products epi asks for where fused_dots is on
+  // and its partials fit; returns whether it did (otherwise the caller runs the separate
+  // dot-product kernels, the default: they measured faster)
+  bool apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
                const DotEpi<P>* epi = nullptr);
   bool fused_dots = false;
   // bounds_zero: the caller guarantees that Y's entries outside the swept interior are

@@ -246,8 +246,6 @@ template void launch_dot<F64>(const double2*, const double2*, long, long, int, c
                               double2*, cudaStream_t);
 template void launch_dot<F32>(const float2*, const float2*, long, long, int, const int*, double2*, int,
                               double2*, cudaStream_t);
-template void launch_dot2<F64>(const double2*, const double2*, const double2*, const double2*, long, long, int,
-                               const int*, double2*, int, double2*, double2*, cudaStream_t);
 template void launch_dot2<F32>(const float2*, const float2*, const float2*, const float2*, long, long, int,
                                const int*, double2*, int, double2*, double2*, cudaStream_t);
 template void launch_xr_dot2<F32>(long, int, const int*, const KrylovScalars*, float2*, const float2*,

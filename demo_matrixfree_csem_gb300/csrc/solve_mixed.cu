@@ -172,7 +172,8 @@ void MixedBatch::inner_iteration(int nact, const int* dl, int preco, int maxiter
   ep.kind = 1;
   ep.e = r0;
   ep.out1 = D + 0 * nsys;
-  o32.apply_A(pp, v, nact, dl, sc, &ep);  // v = A pp, <v, r0>
+  if (!o32.apply_A(pp, v, nact, dl, sc, &ep))  // v = A pp, <v, r0>
+    launch_dot<F32>(v, r0, n, n, nact, dl, part, nblk, D + 0 * nsys, st);
   launch_sc_alpha(nact, dl, K, D + 0 * nsys, st);
   launch_vec<F32>(VEC_S, n, nact, dl, K, r, v, s, nullptr, nullptr, st);
   M(s, sh);
@@ -180,7 +181,8 @@ void MixedBatch::inner_iteration(int nact, const int* dl, int preco, int maxiter
   ep.e = s;
   ep.out1 = D + 1 * nsys;
   ep.out2 = D + 2 * nsys;
-  o32.apply_A(sh, t, nact, dl, sc, &ep);  // t = A sh, <s, t> and <t, t>
+  if (!o32.apply_A(sh, t, nact, dl, sc, &ep))  // t = A sh, <s, t> and <t, t>
+    launch_dot2<F32>(s, t, t, t, n, n, nact, dl, part, nblk, D + 1 * nsys, D + 2 * nsys, st);
   launch_sc_omega(nact, dl, K, D + 1 * nsys, D + 2 * nsys, st);
   launch_xr_dot2<F32>(n, nact, dl, K, d, pp, sh, r, s, t, r0, part, nblk, D + 3 * nsys, D + 4 * nsys, st);
   launch_sc_rs_beta(nact, dl, K, D + 3 * nsys, D + 4 * nsys, nullptr, 0, maxiter, st);
