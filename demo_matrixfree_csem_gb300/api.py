@@ -119,6 +119,7 @@ def lib(build_if_missing: bool = True):
         "csem_profile": (C.c_int, [C.c_int]),
         "csem_profile_read": (C.c_int, [C.c_int, _dp, _lp, _lp]),
         "csem_launch_count": (C.c_longlong, []),
+        "csem_sweep_groups": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, _ip, _ip, _ip, _ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -491,3 +492,15 @@ def cdot(a, b, c64=False) -> complex:
         a, b = _c128(a), _c128(b)
         _check(lib().csem_cdot_host(len(a), _p(a.view(np.float64)), _p(b.view(np.float64)), _p(o)))
     return complex(o[0], o[1])
+
+
+def sweep_groups(iom, ns: int, halves: bool = False):
+    """The same-frequency slot groups of the batched complex64 LU-SGS (csem_sweep_groups):
+    (groups as an (ngroups, ns) array, -1 padded; nA; ngA)."""
+    z = np.asarray(iom, np.complex128).ravel()
+    a = np.ascontiguousarray(np.stack([z.real, z.imag], axis=1).ravel())
+    out = np.zeros(len(z) * ns, np.int32)
+    ng, na, nga = C.c_int(), C.c_int(), C.c_int()
+    _check(lib().csem_sweep_groups(len(z), _p(a), ns, int(bool(halves)), _p(out, _ip), C.byref(ng), C.byref(na),
+                                   C.byref(nga)))
+    return out[:ng.value * ns].reshape(ng.value, ns), na.value, nga.value

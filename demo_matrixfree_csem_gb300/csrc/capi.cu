@@ -275,6 +275,21 @@ int csem_batch_bytes(csem_ctx* c, int precision, int preco, int nsys, double* by
   return CSEM_OK;
 }
 
+int csem_sweep_groups(int nslot, const double* iom, int ns, int halves, int* groups, int* ngroups, int* nA, int* ngA)
+{
+  if (nslot < 1 || ns < 1 || !iom || !groups || !ngroups || !nA || !ngA)
+    return csem_set_error(CSEM_EINVAL, "csem_sweep_groups: bad argument");
+  try {
+    std::vector<int> out;
+    *ngroups = halves ? build_sweep_groups_halves(nslot, iom, ns, 4, out, nA, ngA)
+                      : (*nA = *ngA = 0, build_sweep_groups(nslot, iom, ns, out));
+    memcpy(groups, out.data(), sizeof(int) * out.size());
+  } catch (const std::bad_alloc&) {
+    return csem_set_error(CSEM_ENOMEM, "host allocation failed");
+  }
+  return CSEM_OK;
+}
+
 int csem_batch_capacity(csem_ctx* c, int precision, int preco, double budget_bytes, int* nsys)
 {
   if (!c || !nsys || (precision != 32 && precision != 64))

@@ -167,6 +167,17 @@ int csem_solve_batch_multi(int ndev, const int *devices, const csem_grid_t *g, i
                            const int *chrec, int nrec, const float *rec, const csem_batch_opts *opt, double *dcal,
                            int *iters, int *outer, int *status, double *relres, int *owner);
 
+/* The same-frequency groups the batched complex64 LU-SGS of a set of slots uses (no device
+ * work; for callers planning batches, and for tests): slots with equal iom (re, im pairs
+ * per slot) form groups of at most ns, the slots of one frequency in order, the
+ * frequencies in order of first appearance. halves != 0 and nslot >= 8: built separately
+ * for slots [0, nslot/2) and [nslot/2, nslot), each half numbering its slots from 0, as
+ * the split sweeps on two streams use them; *nA and *ngA are then the first half's slots
+ * and groups (0 otherwise). groups receives *ngroups x ns entries, -1 where a group has
+ * fewer members, and must hold nslot x ns. */
+int csem_sweep_groups(int nslot, const double *iom, int ns, int halves, int *groups, int *ngroups, int *nA,
+                      int *ngA);
+
 /* Capacity planning for large sets of systems (no counterpart in the reference, which
  * solves one system at a time). csem_batch_bytes: device bytes csem_solve_batch_host
  * needs for nsys systems with this precision and preconditioner, beyond the model and

@@ -160,3 +160,26 @@ def test_batch_options_are_checked_before_any_device_work(csem_lib):
     assert call(precision=32, algopt=2, nrestart=0) == EINVAL
     assert call(precision=32, preco=2) == EINVAL
     assert call(precision=16) == EINVAL
+
+
+def test_sweep_groups_partition_the_slots_by_frequency():
+    """csem_sweep_groups: the groups the batched complex64 LU-SGS uses (host logic only)."""
+    from demo_matrixfree_csem_gb300 import api
+    a, b, c = 1j * 3.9e-6, 1j * 5.9e-6, 1j * 7.9e-6
+    iom = [a, b, a, c, a, b, a, a, c]
+    g, na, nga = api.sweep_groups(iom, 2)
+    assert g.tolist() == [[0, 2], [4, 6], [7, -1], [1, 5], [3, 8]] and (na, nga) == (0, 0)
+    g16, _, _ = api.sweep_groups(iom, 16)
+    assert [sorted(x for x in r if x >= 0) for r in g16.tolist()] == [[0, 2, 4, 6, 7], [1, 5], [3, 8]]
+    # two halves of the slots, each numbered from 0 (the split sweeps on two streams)
+    g, na, nga = api.sweep_groups(iom, 2, halves=True)
+    assert (na, nga) == (4, 3)
+    assert g.tolist() == [[0, 2], [1, -1], [3, -1], [0, 2], [3, -1], [1, -1], [4, -1]]
+    for lo, hi, rows in ((0, na, g[:nga]), (na, len(iom), g[nga:])):
+        members = sorted(x for r in rows for x in r if x >= 0)
+        assert members == list(range(hi - lo))
+        for r in rows:
+            assert len({iom[lo + x] for x in r if x >= 0}) == 1
+    # fewer than 8 slots: one set
+    g, na, nga = api.sweep_groups(iom[:7], 4, halves=True)
+    assert (na, nga) == (0, 0) and sorted(x for r in g.tolist() for x in r if x >= 0) == list(range(7))
