@@ -34,6 +34,7 @@ struct csem_ctx {
   bool lusgs_split = true;
   bool lusgs_overlap = true;
   bool fused_dots = false;
+  bool quick_residual = true;
   int lusgs_cap = 0;
   int stencil_by = 8, stencil_ctas = 4;
   bool lusgs_tiled = false;
@@ -196,6 +197,8 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
     c->lusgs_systems = value;
   } else if (!strcmp(name, "lusgs_split")) {
     c->lusgs_split = value != 0;
+  } else if (!strcmp(name, "quick_residual")) {
+    c->quick_residual = value != 0;
   } else if (!strcmp(name, "fused_dots")) {
     c->fused_dots = value != 0;
   } else if (!strcmp(name, "lusgs_overlap")) {
@@ -234,6 +237,7 @@ int csem_ctx_set_option(csem_ctx* c, const char* name, int value)
   if (c->batch) {
     configure(c, c->batch->o64);
     configure(c, c->batch->o32);
+    c->batch->o64.quick_stencil = c->quick_residual;  // the defect correction's residual only
   }
   return CSEM_OK;
 }
@@ -647,6 +651,7 @@ static MixedBatch* batch_for(csem_ctx* c, int nsys)
     c->batch = new MixedBatch(c->model, nsys, c->st);
     configure(c, c->batch->o64);
     configure(c, c->batch->o32);
+    c->batch->o64.quick_stencil = c->quick_residual;  // the defect correction's residual only
   }
   return c->batch;
 }

@@ -41,6 +41,22 @@ struct F32 {
   static constexpr bool exact = false;
 };
 
+// F64Q: complex128 arithmetic without the reference's rounding, for the mixed solver's
+// defect-correction residual r = b - A x, which needs complex128 accuracy but not the
+// reference's bits: spacings enter as reciprocals and FMA contraction is allowed, as in
+// F32. Its grids and per-system scalars have F64's layout (same R and C).
+struct F64Q {
+  typedef double R;
+  typedef double2 C;
+  static __device__ __forceinline__ R add(R a, R b) { return a + b; }
+  static __device__ __forceinline__ R sub(R a, R b) { return a - b; }
+  static __device__ __forceinline__ R mul(R a, R b) { return a * b; }
+  static __device__ __forceinline__ R div(R a, R b) { return a / b; }
+  static __device__ __forceinline__ R divs(R a, R d, R rinv) { (void)d; return a * rinv; }
+  static __device__ __forceinline__ C mk(R x, R y) { return make_double2(x, y); }
+  static constexpr bool exact = false;
+};
+
 // complex helpers over a precision P
 template <class P> __device__ __forceinline__ typename P::C cadd(typename P::C a, typename P::C b)
 { return P::mk(P::add(a.x, b.x), P::add(a.y, b.y)); }
@@ -88,6 +104,20 @@ template <class P> struct GridP {
   const R *r1, *r2, *r3, *r1s, *r2s, *r3s;
   const R *s11, *s22, *s33;
 };
+
+// the same grid seen by another precision with the same real type (F64 -> F64Q)
+template <class Q, class P> inline GridP<Q> grid_as(const GridP<P>& g)
+{
+  static_assert(sizeof(typename Q::R) == sizeof(typename P::R), "grid_as: same real type only");
+  GridP<Q> q;
+  q.n1 = g.n1; q.n2 = g.n2; q.n3 = g.n3; q.n3f = g.n3f; q.nb = g.nb; q.airbc = g.airbc; q.fvm = g.fvm;
+  q.kstart = g.kstart;
+  q.lEx = g.lEx; q.lEy = g.lEy; q.lEz = g.lEz; q.lE = g.lE;
+  q.d1 = g.d1; q.d2 = g.d2; q.d3 = g.d3; q.d1s = g.d1s; q.d2s = g.d2s; q.d3s = g.d3s;
+  q.r1 = g.r1; q.r2 = g.r2; q.r3 = g.r3; q.r1s = g.r1s; q.r2s = g.r2s; q.r3s = g.r3s;
+  q.s11 = g.s11; q.s22 = g.s22; q.s33 = g.s33;
+  return q;
+}
 
 // index maps of the reference layout (fdfd.c:13-21)
 __device__ __forceinline__ long ix1(int n1, int n2, int k, int j, int i) { return i + (long)n1 * (j + (long)(n2 + 1) * k); }

@@ -341,6 +341,13 @@ bool Ops<P>::apply_A(const C* X, C* Y, int nslot, const int* sys_list, const Sys
       return true;
     }
   }
+  if constexpr (P::exact) {
+    if (quick_stencil) {
+      launch_fdfd<F64Q>(grid_as<F64Q>(g), reinterpret_cast<const SysScal<F64Q>*>(sc), X, Y, ghxp, ghyp, nslot,
+                        sys_list, st, stencil_by, stencil_ctas);
+      return false;
+    }
+  }
   launch_fdfd<P>(g, sc, X, Y, ghxp, ghyp, nslot, sys_list, st, stencil_by, stencil_ctas);
   return false;
 }

@@ -158,6 +158,9 @@ class Ops {
   bool apply_A(const C* X, C* Y, int nslot, const int* sys_list, const SysScal<P>* sc,
                const DotEpi<P>* epi = nullptr);
   bool fused_dots = false;
+  // complex128 only: the stencil in F64Q (reciprocal spacings, contraction allowed), for
+  // residuals that need complex128 accuracy but not the reference's bits
+  bool quick_stencil = false;
   // bounds_zero: the caller guarantees that Y's entries outside the swept interior are
   // zero (they are never written by the sweeps, so a buffer only ever written by
   // apply_lusgs, or by operations that keep them zero, stays so); then Y is not cleared

@@ -69,5 +69,7 @@ template <> struct DotAcc<F32> {
   __device__ __forceinline__ double2 value() const { return make_double2(re.value(), im.value()); }
 };
 
+template <> struct DotAcc<F64Q> : DotAcc<F64> {};  // the complex128 accumulation
+
 }  // namespace
 }  // namespace csem

@@ -67,7 +67,7 @@ __device__ __forceinline__ void h_at(const GridP<P>& g, const typename P::C* __r
 // which launch_dot_finish adds up in a fixed order: deterministic, but a different
 // partition of the sum than launch_dot's.
 template <class P, int BY, int EPI>
-__global__ void __launch_bounds__(32 * (BY + 1), P::exact || BY >= 16 ? 1 : CSEM_FDFD_MINB)
+__global__ void __launch_bounds__(32 * (BY + 1), sizeof(typename P::R) == 8 || BY >= 16 ? 1 : CSEM_FDFD_MINB)
 k_fdfd(GridP<P> g, const SysScal<P>* __restrict__ scal, const typename P::C* __restrict__ X,
        typename P::C* __restrict__ Y, const typename P::C* __restrict__ GHX,
        const typename P::C* __restrict__ GHY, int kchunk, int nkc, const int* __restrict__ sys_list,
@@ -376,6 +376,8 @@ template void launch_fdfd<F64>(const GridP<F64>&, const SysScal<F64>*, const dou
                                const double2*, const double2*, int, const int*, cudaStream_t, int, int);
 template void launch_fdfd<F32>(const GridP<F32>&, const SysScal<F32>*, const float2*, float2*,
                                const float2*, const float2*, int, const int*, cudaStream_t, int, int);
+template void launch_fdfd<F64Q>(const GridP<F64Q>&, const SysScal<F64Q>*, const double2*, double2*,
+                                const double2*, const double2*, int, const int*, cudaStream_t, int, int);
 template void launch_hz0<F64>(const GridP<F64>&, const SysScal<F64>*, const double2*, double2*, int,
                               const int*, cudaStream_t);
 template void launch_hz0<F32>(const GridP<F32>&, const SysScal<F32>*, const float2*, float2*, int,

@@ -247,6 +247,13 @@ void *csem_ctx_stream(csem_ctx *c);
  *                     and w = iwmu/aii (once per point for all the systems of a frequency)
  *                     and a row pipeline that reads them and runs only the dependent chain;
  *                     0: the one-pass pipelined sweeps. Same values to rounding;
+ *   "quick_residual"  1 (default): the batched mixed-precision solve forms its complex128
+ *                     residuals r = b - A x with a complex128 stencil that multiplies by
+ *                     reciprocal spacings and lets the compiler contract multiply-adds
+ *                     (complex128 accuracy, not the reference's rounding: the defect
+ *                     correction needs no more); 0: the bit-faithful complex128 stencil.
+ *                     The complex128 solver (precision 64) and the operator entry points
+ *                     always use the bit-faithful one;
  *   "fused_dots"      1: the batched complex64 BiCGStab forms v.r0 after v = A p and s.t,
  *                     t.t after t = A s inside the operator's stencil (one deterministic
  *                     partial per CTA); 0 (default): separate dot-product passes, which
