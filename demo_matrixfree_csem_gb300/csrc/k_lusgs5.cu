@@ -19,6 +19,12 @@
 // coalesced pass leaves the sweep one such access per point instead of up to twelve.
 // B and w are the expressions of k_sweep_ex32 / k_sweep_eyz32's make(), so the values
 // are those sweeps' up to the compiler's multiply-add contraction.
+//
+// The pass takes groups of slots at one frequency (a thread forms the point's 1/aii and w
+// once for the group); the pipeline is instantiated per warp count so that its pairwise
+// barrier ids are immediates (2 NW - 1 hardware barriers per CTA instead of 16), and may
+// run a capped grid whose CTAs take lines in turn. Engine side (Ops::apply_lusgs): batches
+// of 8 or more systems run as two halves on two streams.
 #include "csem_cuda.cuh"
 #include "engine.h"
 #include "k_sweep_common.cuh"
