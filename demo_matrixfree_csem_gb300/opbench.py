@@ -1,7 +1,14 @@
 """Operator micro-benchmark: time A, LU-SGS or A-phi applications on a batch of systems.
 
     python -m demo_matrixfree_csem_gb300.opbench --workload marlim_like_96 --op lusgs \
-        --prec 32 --nsys 16 --reps 5 [--schedule pipelined|diagonal] [--vw 0|1|2|4]
+        --prec 32 --nsys 16 --reps 5 [--schedule pipelined|diagonal] [--vw 0|1|2|4] \
+        [--split 1|0] [--overlap 1|0] [--cap N] [--systems 1|2|4] [--lines N] [--tiled 0|1] \
+        [--by 4|8|16] [--ctas N]
+
+The schedule flags set the context options of the same names (lusgs_split, lusgs_overlap,
+lusgs_cap, lusgs_systems, lusgs_lines, lusgs_tiled, stencil_by, stencil_ctas); the
+defaults are the library's. All systems of one call share one frequency (--freq), so the
+grouped schedules see full groups.
 
 --op csr compares the matrix-free operator with the same operator assembled in CSR and
 applied by cuSPARSE (csem_csr_compare), on the workload's grid without the airwave (the
