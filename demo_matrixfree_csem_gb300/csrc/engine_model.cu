@@ -468,7 +468,9 @@ void Ops<P>::apply_lusgs(const C* X, C* Y, int nslot, const int* sys_list, const
       if (split_sweeps && pipelined_sweeps && sweep_pipelined_fits(comp, n1, n2, s.nK)) {
         const long sbs = sweep_split_scratch(n1, n2, s.nK);
         if (sb.bytes < sizeof(float4) * (size_t)sbs * nmax) sb.alloc(sizeof(float4) * (size_t)sbs * nmax);
-        const bool g16 = grp && grp->ns == SPLIT_GROUP && grp->n > 0;
+        // groups built as two halves number their slots within each half: here, on one
+        // stream, the pass then takes the slots one by one
+        const bool g16 = grp && grp->ns == SPLIT_GROUP && grp->n > 0 && grp->nA == 0;
         launch_sweep_split(s, comp, fwd, nslot, sb.as<float4>(), sbs, sweep_vw == 1 || sweep_vw == 4 ? sweep_vw : 2,
                            g16 ? grp->dev : nullptr, g16 ? grp->n : 0, g16 ? grp->ns : 1, st);
         return;
