@@ -236,7 +236,7 @@ void extract_emf(acq_t *acq, emf_t *emf, csem_z *x, int ifreq)
     rec[5 * r + 3] = acq->rec_azimuth ? acq->rec_azimuth[r] : 0.f;
     rec[5 * r + 4] = acq->rec_dip ? acq->rec_dip[r] : 0.f;
   }
-  int *ch = (int *)malloc(sizeof(int) * (size_t)(nch > 0 ? nch : 1));
+  int *ch = (int *)calloc((size_t)(nch > 0 ? nch : 1), sizeof(int));
   for (int c = 0; c < nch; c++) ch[c] = channel_code(emf->chrec[c]);
   double *out = (double *)malloc(sizeof(double) * 2 * (size_t)nch * (nrec > 0 ? nrec : 1));
   if (csem_extract_host(g_ctx, nch, ch, nrec, rec, (const double *)x, out)) fail("extract_emf");

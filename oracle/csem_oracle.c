@@ -589,8 +589,6 @@ void orc_aphi_apply(orc_ctx_t *c, const double *x, double *y)
   R.bx = x; R.by = x + 2 * c->lEx; R.bz = x + 2 * (c->lEx + c->lEy);
   double *v = c->v, *bv = c->bv;
   const double *d1 = R.d1, *d2 = R.d2, *d3 = R.d3, *d1s = R.d1s, *d2s = R.d2s, *d3s = R.d3s;
-  const rows_t *Rp = &R;
-#define RR (Rp)
   memset(bv, 0, sizeof(double) * 2 * (size_t)c->lv);
   for (int k = 1; k < n3; k++)
     for (int j = 1; j < n2; j++)
@@ -602,7 +600,6 @@ void orc_aphi_apply(orc_ctx_t *c, const double *x, double *y)
         s = cadd(s, cdivr(cneg(csub(ld(R.bz, p), ld(R.bz, ((long)(k - 1) * (n2 + 1) + j) * (n1 + 1) + i))), d3[k]));
         st(bv, p, s);
       }
-#undef RR
   memset(y, 0, sizeof(double) * 2 * (size_t)c->lE);
   memset(v, 0, sizeof(double) * 2 * (size_t)c->lv);
   /* forward: ax, ay, az with v = 0 (v terms vanish), then v */
