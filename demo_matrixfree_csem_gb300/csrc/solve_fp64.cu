@@ -118,7 +118,6 @@ int Solver64::fbicgstab(int precond, int mp, double2* x, const double2* b, int n
   KrylovScalars kh;
   CSEM_CUDA_TRY(cudaMemcpyAsync(&kh, K, sizeof(kh), cudaMemcpyDeviceToHost, st));
   CSEM_CUDA_TRY(cudaStreamSynchronize(st));
-  int iter = 0;
   if (kh.status == ST_RUNNING && niter <= 0) kh.status = ST_MAXITER;
   while (kh.status == ST_RUNNING) {
     if (flexible) {
@@ -147,7 +146,6 @@ int Solver64::fbicgstab(int precond, int mp, double2* x, const double2* b, int n
     launch_sc_rs_beta(1, nullptr, K, d + 5, d + 6, hist.as<double>(), hcap, niter, st);
     CSEM_CUDA_TRY(cudaMemcpyAsync(&kh, K, sizeof(kh), cudaMemcpyDeviceToHost, st));
     CSEM_CUDA_TRY(cudaStreamSynchronize(st));
-    iter = kh.iter;
     if (kh.status != ST_RUNNING) break;
     launch_vec<F64>(VEC_P, n, 1, nullptr, K, r, p, v, nullptr, nullptr, st);
   }

@@ -22,9 +22,10 @@
 
 namespace csem {
 
+// (r and r0 may be the same vector: the GMRES start writes r0 through both)
 __global__ void k_start_inner(long n, const int* __restrict__ list, const double* __restrict__ rn,
-                              const double2* __restrict__ r64, float2* __restrict__ r, float2* __restrict__ r0,
-                              float2* __restrict__ p, float2* __restrict__ d)
+                              const double2* __restrict__ r64, float2* r, float2* r0, float2* __restrict__ p,
+                              float2* __restrict__ d)
 {
   const int sys = list[blockIdx.y];
   const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
